@@ -1,0 +1,123 @@
+"""ctypes binding of libqms_gb300.so (declarations in include/qms.h).
+
+The library must have been built (``python -m alpineqms_gb300.build`` or
+``__graft_entry__.build()``); there is no fallback implementation, so a
+missing library raises ``QMSLibraryError`` instead of computing anything on
+the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from .build import LIB
+
+_lock = threading.Lock()
+_lib = None
+
+
+class QMSLibraryError(RuntimeError):
+    pass
+
+
+class QmsDesc(ctypes.Structure):
+    _fields_ = [("xs", ctypes.c_int), ("ys", ctypes.c_int), ("zs", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("dt", ctypes.c_double),
+                ("precision", ctypes.c_int),
+                ("tol", ctypes.c_double),
+                ("max_outer", ctypes.c_int),
+                ("max_inner", ctypes.c_int),
+                ("inner_rtol", ctypes.c_double),
+                ("check_every", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class QmsStats(ctypes.Structure):
+    _fields_ = [("outer_iterations", ctypes.c_int),
+                ("inner_iterations", ctypes.c_int),
+                ("initial_residual", ctypes.c_double),
+                ("final_residual", ctypes.c_double),
+                ("status", ctypes.c_uint)]
+
+
+class QmsProfile(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_int64),
+                ("op32_launches", ctypes.c_int64), ("op32_ms", ctypes.c_double), ("op32_bytes", ctypes.c_double),
+                ("op64_launches", ctypes.c_int64), ("op64_ms", ctypes.c_double), ("op64_bytes", ctypes.c_double)]
+
+
+QMS_PREC_MIXED, QMS_PREC_FP64 = 0, 1
+QMS_FIELD_CUBES, QMS_FIELD_SLICE = 0, 1
+ERRORS = {-1: "QMS_ERR_ARG", -2: "QMS_ERR_CUDA", -3: "QMS_ERR_NOMEM", -4: "QMS_ERR_STATE", -5: "QMS_ERR_CONVERGE"}
+
+# (name, restype, argtypes) -- the full export table of include/qms.h
+_VP = ctypes.c_void_p
+_DP = ctypes.POINTER(ctypes.c_double)
+_H = ctypes.c_void_p
+SIGNATURES = [
+    ("qms_default_desc", None, [ctypes.POINTER(QmsDesc), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    ("qms_device_bytes", ctypes.c_size_t, [ctypes.POINTER(QmsDesc)]),
+    ("qms_n_dims", ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("qms_csr_nnz", ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("qms_create", ctypes.c_int, [ctypes.POINTER(QmsDesc), ctypes.POINTER(_H)]),
+    ("qms_destroy", None, [_H]),
+    ("qms_last_error", ctypes.c_char_p, [_H]),
+    ("qms_set_materials", ctypes.c_int, [_H, _VP, _VP, ctypes.c_int]),
+    ("qms_set_geometry_f64", ctypes.c_int, [_H, _VP, _VP, ctypes.c_int]),
+    ("qms_steady", ctypes.c_int, [_H, _DP, _DP, _DP]),
+    ("qms_step", ctypes.c_int, [_H, _DP, _DP, _DP]),
+    ("qms_get_stats", ctypes.c_int, [_H, ctypes.POINTER(QmsStats)]),
+    ("qms_get_fields", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP]),
+    ("qms_get_state", ctypes.c_int, [_H, _VP]),
+    ("qms_set_state", ctypes.c_int, [_H, _VP]),
+    ("qms_assemble_csr", ctypes.c_int, [_H, ctypes.c_int, _DP, _DP, _DP, _VP, _VP, _VP, _VP, _VP]),
+    ("qms_apply", ctypes.c_int, [_H, ctypes.c_int, _DP, ctypes.c_int, _VP, _VP]),
+    ("qms_csr_spmv", ctypes.c_int, [_H, _VP, _VP, _VP, _VP, _VP]),
+    ("qms_residual_norm", ctypes.c_int, [_H, ctypes.c_int, _DP, _DP]),
+    ("qms_profile_enable", ctypes.c_int, [_H, ctypes.c_int]),
+    ("qms_get_profile", ctypes.c_int, [_H, ctypes.POINTER(QmsProfile)]),
+    ("qms_get_stream", ctypes.c_void_p, [_H]),
+]
+
+
+def lib_path() -> str:
+    return LIB
+
+
+def load():
+    """Load libqms_gb300.so (raises QMSLibraryError when it was not built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB):
+                raise QMSLibraryError(f"{LIB} is missing; build it with `python -m alpineqms_gb300.build`")
+            L = ctypes.CDLL(LIB)
+            for name, res, args in SIGNATURES:
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(rc: int, handle=None, what: str = ""):
+    if rc == 0:
+        return
+    L = load()
+    msg = L.qms_last_error(handle)
+    msg = msg.decode() if msg else ""
+    raise QMSError(rc, f"{what}: {ERRORS.get(rc, rc)}: {msg}")
+
+
+class QMSError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+def dvec(values):
+    arr = (ctypes.c_double * len(values))(*[float(v) for v in values])
+    return arr

@@ -1,0 +1,76 @@
+// qms_solver.h -- the solver object behind a qms_handle.
+#pragma once
+#include "qms.h"
+#include "qms_internal.h"
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#define QMS_NVEC 7
+
+size_t qms_device_bytes_impl(const qms_desc& d);
+
+struct QmsSolver {
+    qms_desc desc{};
+    QGrid g{};
+    int dev = -1;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    bool fp64_inner = false;
+    size_t tsize = 4;
+    long long vec_blocks = 0, nbop = 0;
+
+    uint8_t* ids = nullptr;
+    QMatTable<double> htab64{};
+    QMatTable<float> htab32{};
+    QMatTable<double>* dtab64 = nullptr;
+    QMatTable<float>* dtab32 = nullptr;
+    double* x = nullptr;        // current solution [Ax|Ay|Az|V]
+    double* b = nullptr;        // RHS of the last solve
+    double* r64 = nullptr;      // scaled FP64 residual
+    double* H = nullptr;        // Hx|Hy|Hz cubes
+    double* slicebuf = nullptr;
+    double* part = nullptr;     // block partial sums
+    double* S = nullptr;        // device scalars
+    double* hS = nullptr;       // pinned host mirror
+    unsigned* status = nullptr;
+    float* dg_steady = nullptr; // Jacobi diagonals
+    float* dg_tr = nullptr;
+    void* vec[QMS_NVEC] = {};   // inner Krylov vectors (FP32 or FP64)
+
+    qms_stats stats{};
+    std::string err;
+
+    // instrumentation (qms_profile_enable)
+    bool prof = false;
+    long long nlaunch = 0;
+    struct OpEv { cudaEvent_t a, b; int fp64; double bytes; };
+    std::vector<OpEv> evpool;
+    size_t evused = 0;
+    qms_profile profacc{};
+    int profile_enable(bool on);
+    int profile_collect(qms_profile* out);
+    template <typename T>
+    void op(bool adv, int mode, const QStepPar<T>& P, const T* x, const T* b, T* y, const T* w, double* partials);
+
+    ~QmsSolver();
+    void release();
+    int init(const qms_desc& d);
+    int set_materials(const uint8_t* host_slots, const double* rows6, int nmat);
+    int solve(bool transient, const double v[3], const double B[3], const double G[9]);
+    int residual(bool adv, bool transient, const double v[3]);
+    int fields(int which, int axis, int index, double* host_out);
+    int finalize(int op, int nsum, long long nb);
+    int read_scalars();
+
+    QCoef<float> coef32() const;
+    QCoef<double> coef64() const;
+    template <typename T> QCoef<T> coef() const;
+
+    template <typename T> int inner_bicgstab(bool adv, bool transient, const double v[3], int& iters);
+    template <typename T> int inner_pcg(bool transient, int& iters);
+};
+
+template <> inline QCoef<float> QmsSolver::coef<float>() const { return coef32(); }
+template <> inline QCoef<double> QmsSolver::coef<double>() const { return coef64(); }

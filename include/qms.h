@@ -1,0 +1,163 @@
+/*
+ * qms.h -- C-ABI of libqms_gb300.so, the GB300 implementation of the
+ * AlpineQMS QMS_3D per-step hot path (Yee-grid A-V assembly and solve).
+ *
+ * The reference has no library boundary: 3D/master.py:84 runs the Fortran
+ * executable (`./QMS_3D inputs.txt`) and the program calls MKL PARDISO on a
+ * CSR matrix it assembles itself.  The entry points below replace, one for
+ * one, the pieces of that program (3D/QMS_3D.f90, cited as F:line):
+ *
+ *   qms_create / qms_destroy        allocation of fields, CSR and PARDISO
+ *                                   handles (F:286-357, F:398-405) and the
+ *                                   final release (F:2315-2318)
+ *   qms_set_materials               material table -> Yee coefficients
+ *                                   (F:193-279); geometry as uint8 slots
+ *   qms_set_geometry_f64            geom.bin float64 IDs + table lookup
+ *                                   (F:229-254), converted on the GPU
+ *   qms_steady                      steady-state assembly + phase-13 solve
+ *                                   (F:430-1317)
+ *   qms_step                        one backward-Euler step: assembly +
+ *                                   phase-23/33 solve (F:1451-2208)
+ *   qms_get_fields                  unpack + H at cell centres + slice
+ *                                   (F:1319-1394, F:2210-2290)
+ *   qms_get_state / qms_set_state   the x_vec solution [Ax|Ay|Az|V] (F:1316)
+ *   qms_assemble_csr                the CSR matrix and RHS handed to PARDISO
+ *                                   (F:448-1312 steady, F:1457-2191
+ *                                   transient), bit-exact; verification path
+ *   qms_apply                       y = M x with the matrix-free operator
+ *   qms_residual_norm               ||D^-1 (b - M x)|| of the current state
+ *
+ * Conventions: every function returns 0 on success and a negative QMS_ERR_*
+ * code otherwise (no exceptions cross the ABI); qms_last_error() gives the
+ * message.  Host pointers are borrowed for the duration of the call.  Device
+ * pointers (d_*) must be allocations on the handle's device.  A handle is
+ * used by one host thread at a time.  Velocities are the frame velocity
+ * solve_v{x,y,z} of the step (F:431-433, F:1447-1449); B and G are the
+ * background field and its 3x3 gradient (row-major gxx gxy gxz gyx ... gzz)
+ * in effect for that solve.
+ */
+#ifndef QMS_GB300_H
+#define QMS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QMS_ABI_VERSION 1
+
+enum {
+    QMS_OK = 0,
+    QMS_ERR_ARG = -1,        /* invalid argument / size */
+    QMS_ERR_CUDA = -2,       /* CUDA runtime error */
+    QMS_ERR_NOMEM = -3,      /* device allocation failed */
+    QMS_ERR_STATE = -4,      /* call out of order */
+    QMS_ERR_CONVERGE = -5    /* solver did not reach the tolerance (state kept) */
+};
+
+enum { QMS_PREC_MIXED = 0, QMS_PREC_FP64 = 1 };
+enum { QMS_FIELD_CUBES = 0, QMS_FIELD_SLICE = 1 };
+
+/* status bits reported in qms_stats.status */
+enum {
+    QMS_STATUS_BAD_MATERIAL = 1,
+    QMS_STATUS_NAN = 2,
+    QMS_STATUS_NO_CONVERGENCE = 4,
+    QMS_STATUS_BREAKDOWN = 8
+};
+
+typedef struct {
+    int xs, ys, zs;          /* cells per axis (F:123) */
+    double dx, dy, dz;       /* cell size, m (F:124) */
+    double dt;               /* time step, s (F:125) */
+    int precision;           /* QMS_PREC_MIXED: FP32 inner Krylov in FP64 refinement;
+                                QMS_PREC_FP64: the same solver entirely in FP64 */
+    double tol;              /* stop when ||D^-1 (b - M x)|| <= tol * ||x|| */
+    int max_outer;           /* refinement iterations */
+    int max_inner;           /* Krylov iterations per refinement iteration */
+    double inner_rtol;       /* relative reduction asked of each inner solve */
+    int check_every;         /* inner iterations between host convergence checks */
+    int device;              /* CUDA device ordinal */
+} qms_desc;
+
+typedef struct {
+    int outer_iterations;
+    int inner_iterations;
+    double initial_residual; /* relative scaled residual before the solve */
+    double final_residual;   /* after */
+    unsigned status;         /* QMS_STATUS_* bits */
+} qms_stats;
+
+typedef struct qms_handle qms_handle;
+
+/* Fills `d` with the defaults for a grid (mixed precision, tol 1e-12). */
+void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy, double dz, double dt);
+/* Device bytes a handle with this descriptor allocates (admission control). */
+size_t qms_device_bytes(const qms_desc* d);
+int64_t qms_n_dims(int xs, int ys, int zs);
+int64_t qms_csr_nnz(int xs, int ys, int zs);
+
+int qms_create(const qms_desc* d, qms_handle** out);
+void qms_destroy(qms_handle* h);
+const char* qms_last_error(const qms_handle* h);   /* h may be NULL: last create error */
+
+/* slots: xs*ys*zs uint8 in Fortran order, 0 = vacuum, r = row r of `rows`;
+ * rows: nmat x 6 doubles (mu_r x,y,z, sigma x,y,z), nmat <= 255 */
+int qms_set_materials(qms_handle* h, const uint8_t* slots, const double* rows, int nmat);
+/* geom: xs*ys*zs float64 material IDs (geom.bin); table: nmat x 7 doubles
+ * (ID, mu_r x,y,z, sigma x,y,z) as read from inputs.txt (F:157-161).  IDs absent
+ * from the table are vacuum; IDs above the table maximum or negative are
+ * rejected (QMS_ERR_ARG). */
+int qms_set_geometry_f64(qms_handle* h, const double* geom, const double* table, int nmat);
+
+int qms_steady(qms_handle* h, const double v[3], const double B[3], const double G[9]);
+int qms_step(qms_handle* h, const double v[3], const double B[3], const double G[9]);
+int qms_get_stats(const qms_handle* h, qms_stats* out);
+
+/* which = QMS_FIELD_CUBES: out = Hx|Hy|Hz cubes (3*xs*ys*zs doubles, F-order);
+ * which = QMS_FIELD_SLICE: out = the three slices (axis 0/1/2 = x/y/z, 1-based
+ * index), each in the record layout of F:1380-1394. */
+int qms_get_fields(qms_handle* h, int which, int axis, int index, double* out);
+int qms_get_state(qms_handle* h, double* x_out);          /* n_dims doubles */
+int qms_set_state(qms_handle* h, const double* x_in);
+
+/* Verification path: CSR of the steady (transient = 0) or transient system and
+ * its RHS, bit-identical to the reference's (F:448-1312 / F:1457-2191).
+ * d_ia: n_dims+1 int64 (1-based), d_ja: nnz int32 (1-based), d_a: nnz doubles,
+ * d_b: n_dims doubles, d_xprev: previous solution (transient only).  The int64
+ * row pointer replaces the reference's int32 one (which overflows above
+ * ~2^31 non-zeros). */
+int qms_assemble_csr(qms_handle* h, int transient, const double v[3], const double B[3], const double G[9],
+                     const double* d_xprev, int64_t* d_ia, int32_t* d_ja, double* d_a, double* d_b);
+/* y = M x with the matrix-free operator in FP64 (fp32 = 0) or FP32 (fp32 = 1);
+ * d_x, d_y: n_dims elements of that type. */
+int qms_apply(qms_handle* h, int transient, const double v[3], int fp32, const void* d_x, void* d_y);
+/* CSR SpMV on the verification-path arrays (FP64). */
+int qms_csr_spmv(qms_handle* h, const int64_t* d_ia, const int32_t* d_ja, const double* d_a, const double* d_x,
+                 double* d_y);
+/* ||D^-1 (b - M x)||_2 / ||x||_2 for the current state and the RHS of the last solve. */
+int qms_residual_norm(qms_handle* h, int transient, const double v[3], double* rel_out);
+
+/* Instrumentation for benchmarks: when enabled, every operator launch is
+ * bracketed by CUDA events on the handle's stream, and every kernel launch of
+ * the handle is counted.  Enabling resets the counters. */
+typedef struct {
+    int64_t launches;        /* all kernel launches since the reset */
+    int64_t op32_launches;   /* FP32 operator applications */
+    double op32_ms;          /* their summed device time */
+    double op32_bytes;       /* their summed algorithmic bytes (x, y, dot vector, material slots) */
+    int64_t op64_launches;   /* FP64 operator applications (residuals) */
+    double op64_ms;
+    double op64_bytes;
+} qms_profile;
+int qms_profile_enable(qms_handle* h, int on);
+int qms_get_profile(qms_handle* h, qms_profile* out);
+/* The cudaStream_t all work of the handle runs on (to record events around calls). */
+void* qms_get_stream(qms_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,69 @@
+"""C-ABI checks that need no GPU: the library loads, exports every function
+include/qms.h declares, and its host-only size functions agree with the oracle."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import qms_oracle as o
+from conftest import ROOT
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "qms.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(qms_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from alpineqms_gb300 import build as b, _lib
+    b.build()
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = header_functions()
+    assert len(names) >= 19
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_binding_table_matches_header():
+    from alpineqms_gb300 import _lib
+    bound = {s[0] for s in _lib.SIGNATURES}
+    assert bound == set(header_functions())
+
+
+@pytest.mark.parametrize("shape", [(6, 7, 8), (32, 32, 32), (17, 9, 23), (96, 96, 96), (128, 64, 32)])
+def test_sizes_agree_with_oracle(lib, shape):
+    n, nnz, _ = o.sizes(*shape)
+    assert lib.qms_n_dims(*shape) == n
+    assert lib.qms_csr_nnz(*shape) == nnz
+
+
+def test_device_bytes_monotone(lib):
+    from alpineqms_gb300._lib import QmsDesc
+    d = QmsDesc()
+    lib.qms_default_desc(ctypes.byref(d), 64, 64, 64, 1e-3, 1e-3, 1e-3, 1e-5)
+    b64 = lib.qms_device_bytes(ctypes.byref(d))
+    lib.qms_default_desc(ctypes.byref(d), 128, 128, 128, 1e-3, 1e-3, 1e-3, 1e-5)
+    b128 = lib.qms_device_bytes(ctypes.byref(d))
+    assert 7 * b64 < b128 < 9 * b64
+    d.precision = 1
+    assert lib.qms_device_bytes(ctypes.byref(d)) > b128
+
+
+def test_create_without_gpu_fails_cleanly(lib):
+    """No exception crosses the ABI: a failing create returns a code and a message."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from alpineqms_gb300._lib import QmsDesc
+    d = QmsDesc()
+    lib.qms_default_desc(ctypes.byref(d), 8, 8, 8, 1e-3, 1e-3, 1e-3, 1e-5)
+    h = ctypes.c_void_p()
+    rc = lib.qms_create(ctypes.byref(d), ctypes.byref(h))
+    assert rc < 0 and not h.value
+    assert lib.qms_last_error(None)

@@ -1,0 +1,217 @@
+"""GPU path vs the CPU oracle, through the C-ABI (libqms_gb300.so).
+
+* K1 CSR assembly: ia/ja/a/b bit-identical to the oracle (which is itself
+  bit-identical to the reference program, test_oracle_golden.py).
+* K2 matrix-free operator vs the assembled CSR (FP64 to 1e-13, FP32 to 1e-5).
+* K7 RHS and K8 H bit-identical to the oracle.
+* Whole steady + transient solves vs the oracle's direct solve: rel-L2 <= 1e-8
+  for A, H (B/mu) and the edge current sigma*grad V (V itself carries the
+  floating constant of isolated conductors, see qms_oracle.DirectSolver).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import qms_oracle as o
+from conftest import GOLDEN_CASES, load_golden
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from alpineqms_gb300 import _lib
+    _lib.load()
+
+
+def rel_l2(a, b, floor=0.0):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), floor))
+
+
+def make_case(xs, ys, zs, seed=0, nmat=3, dxyz=(1e-3, 1.1e-3, 0.9e-3)):
+    rng = np.random.default_rng(seed)
+    geom = rng.integers(0, nmat + 1, size=(xs, ys, zs)).astype(np.float64)
+    props = np.array([[m + 1, *(10 ** rng.uniform(0, 3, 3)), *(10 ** rng.uniform(5, 7.7, 3))] for m in range(nmat)])
+    return geom.flatten(order="F"), props, dxyz
+
+
+def solver_for(xs, ys, zs, d, dt, geom, props, **kw):
+    from alpineqms_gb300.solver import QMSSolver, default_desc
+    s = QMSSolver(default_desc(xs, ys, zs, *d, dt, **kw))
+    s.set_geometry_f64(geom, props)
+    return s
+
+
+CSR_CASES = [
+    (6, 7, 8, dict(v=(0.0, 0.0, 0.0), B=(0, 0, 1e-3), G=np.zeros(9))),
+    (9, 8, 7, dict(v=(1.5, -0.5, 0.25), B=(2e-3, -1e-3, 5e-3), G=[0.05, 0.02, -0.01, 0.02, -0.03, 0.04, -0.01, 0.04, -0.02])),
+    (17, 13, 11, dict(v=(-10.0, 0.0, 2.0), B=(1e-2, 0, 0), G=[0, 0, 0.1, 0, -0.05, 0, 0.1, 0, -0.05])),
+]
+
+
+@pytest.mark.parametrize("xs,ys,zs,par", CSR_CASES)
+@pytest.mark.parametrize("transient", [False, True])
+def test_csr_assembly_bit_exact(xs, ys, zs, par, transient):
+    geom, props, d = make_case(xs, ys, zs, seed=xs)
+    dt = 2e-5
+    n, nnz, _ = o.sizes(xs, ys, zs)
+    rng = np.random.default_rng(1)
+    xp = rng.standard_normal(n) * 1e-3
+    c = o.materials(xs, ys, zs, geom, props)
+    ia, ja, a, b = o.assemble(xs, ys, zs, *d, c, transient, dt, par["v"], par["B"], par["G"], xp)
+    s = solver_for(xs, ys, zs, d, dt, geom, props)
+    dev = "cuda"
+    t_ia = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    t_ja = torch.empty(nnz, dtype=torch.int32, device=dev)
+    t_a = torch.empty(nnz, dtype=torch.float64, device=dev)
+    t_b = torch.empty(n, dtype=torch.float64, device=dev)
+    t_x = torch.from_numpy(xp).to(dev)
+    s.assemble_csr(transient, par["v"], par["B"], par["G"], t_x.data_ptr(), t_ia.data_ptr(), t_ja.data_ptr(),
+                   t_a.data_ptr(), t_b.data_ptr())
+    assert np.array_equal(t_ia.cpu().numpy(), ia.astype(np.int64))
+    assert np.array_equal(t_ja.cpu().numpy(), ja)
+    assert np.array_equal(t_a.cpu().numpy(), a)
+    assert np.array_equal(t_b.cpu().numpy(), b)
+    s.close()
+
+
+def test_csr_assembly_golden_inputs():
+    """The GPU CSR of the steady system for each golden case equals the reference program's."""
+    from alpineqms_gb300.inputs import parse_inputs_text
+    for name in GOLDEN_CASES:
+        z = load_golden(name)
+        inp = parse_inputs_text(bytes(z["inputs_txt"]).decode())
+        n = inp.n_dims
+        nnz = len(z["ja"])
+        v = [t.v0 for t in inp.traj]
+        s = solver_for(inp.xs, inp.ys, inp.zs, (inp.dx, inp.dy, inp.dz), inp.dt, z["geom"].flatten(order="F"),
+                       inp.props_table())
+        t_ia = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+        t_ja = torch.empty(nnz, dtype=torch.int32, device="cuda")
+        t_a = torch.empty(nnz, dtype=torch.float64, device="cuda")
+        t_b = torch.empty(n, dtype=torch.float64, device="cuda")
+        s.assemble_csr(False, v, inp.B, inp.G_flat, 0, t_ia.data_ptr(), t_ja.data_ptr(), t_a.data_ptr(),
+                       t_b.data_ptr())
+        assert np.array_equal(t_ia.cpu().numpy(), z["ia"].astype(np.int64)), name
+        assert np.array_equal(t_ja.cpu().numpy(), z["ja"]), name
+        assert np.array_equal(t_a.cpu().numpy(), z["a0"]), name
+        assert np.array_equal(t_b.cpu().numpy(), z["b0"]), name
+        s.close()
+
+
+@pytest.mark.parametrize("xs,ys,zs,par", CSR_CASES)
+@pytest.mark.parametrize("transient", [False, True])
+def test_matrix_free_operator_vs_csr(xs, ys, zs, par, transient):
+    geom, props, d = make_case(xs, ys, zs, seed=xs + 1)
+    dt = 2e-5
+    n, nnz, _ = o.sizes(xs, ys, zs)
+    c = o.materials(xs, ys, zs, geom, props)
+    ia, ja, a, _ = o.assemble(xs, ys, zs, *d, c, transient, dt, par["v"], par["B"], par["G"], np.zeros(n))
+    A = o.to_scipy(ia, ja, a, n)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(n) * 1e-3
+    yref = A @ x
+    s = solver_for(xs, ys, zs, d, dt, geom, props)
+    tx = torch.from_numpy(x).cuda()
+    ty = torch.empty_like(tx)
+    s.apply(transient, par["v"], False, tx.data_ptr(), ty.data_ptr())
+    y = ty.cpu().numpy()
+    # per-row scale: sum |a_ij x_j| (entries differ from the CSR by a few ulp)
+    Aabs = o.to_scipy(ia, ja, np.abs(a), n)
+    scale = Aabs @ np.abs(x)
+    assert np.max(np.abs(y - yref) / scale) < 1e-13
+    tx32 = tx.float()
+    ty32 = torch.empty_like(tx32)
+    s.apply(transient, par["v"], True, tx32.data_ptr(), ty32.data_ptr())
+    assert np.max(np.abs(ty32.cpu().double().numpy() - yref) / scale) < 2e-5
+    s.close()
+
+
+def test_rhs_and_hfield_bit_exact():
+    """K7 (via a steady/transient solve's b) and K8 equal the oracle's values for the same x."""
+    xs, ys, zs = 10, 9, 11
+    geom, props, d = make_case(xs, ys, zs, seed=5)
+    dt = 1e-5
+    c = o.materials(xs, ys, zs, geom, props)
+    n = o.sizes(xs, ys, zs)[0]
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(n) * 1e-3
+    s = solver_for(xs, ys, zs, d, dt, geom, props)
+    s.set_state(x)
+    H = s.fields()
+    Hr = o.hfield(xs, ys, zs, *d, c, x)
+    for q in range(3):
+        assert np.array_equal(H[q].ravel(order="F"), Hr[q])
+    sl = s.slices("y", 4)
+    for q in range(3):
+        assert np.array_equal(sl[q], H[q][:, 3, :])
+    s.close()
+
+
+def _run_gpu(p, geom, precision, steps, **kw):
+    from alpineqms_gb300.trajectory import VelocitySchedule, scaled_field
+    from alpineqms_gb300.inputs import Trajectory
+    traj = [Trajectory(1, *t) for t in p["traj"]]
+    sched = VelocitySchedule(traj, p["dt"])
+    out = []
+    s = solver_for(p["xs"], p["ys"], p["zs"], (p["dx"], p["dy"], p["dz"]), p["dt"], geom, p["props"],
+                   precision=precision, **kw)
+    B, G = scaled_field(p["B"], p["G"], p.get("excitation"), 0.0)
+    st = s.steady(sched.steady(), B, G)
+    out.append((s.get_state(), [h.ravel(order="F") for h in s.fields()], st))
+    for n in range(1, steps + 1):
+        v = sched.step(n)
+        B, G = scaled_field(p["B"], p["G"], p.get("excitation"), n * p["dt"])
+        st = s.step(v, B, G)
+        out.append((s.get_state(), [h.ravel(order="F") for h in s.fields()], st))
+    s.close()
+    return out
+
+
+def _conductor_case(moving):
+    xs, ys, zs = 16, 14, 12
+    geom = np.zeros((xs, ys, zs))
+    geom[4:12, 4:10, 4:8] = 1
+    geom[6:9, 6:8, 5:7] = 2
+    props = np.array([[1, 1, 1, 1, 3.5e7, 3.5e7, 3.5e7], [2, 200, 200, 200, 2e6, 2e6, 2e6]], np.float64)
+    traj = [(0.0, -1e6, 1), (0.0, 0.0, 0), (0.0, 0.0, 0)] if moving else [(0.0, 0.0, 0)] * 3
+    p = dict(xs=xs, ys=ys, zs=zs, dx=1e-3, dy=1e-3, dz=1e-3, dt=1e-5, Nt=3, B=(1e-3, 2e-3, 1e-2),
+             G=np.array([[-0.05, 0, 0], [0, -0.05, 0], [0, 0, 0.1]]), traj=traj, props=props,
+             excitation=None if moving else ("cos", 1000.0, 0.0))
+    return p, geom.flatten(order="F")
+
+
+@pytest.mark.parametrize("moving", [False, True])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solve_matches_direct_oracle(moving, precision):
+    p, geom = _conductor_case(moving)
+    ref = o.simulate(p, geom, steps=3, keep_states=True)
+    got = _run_gpu(p, geom, precision, 3)
+    c = o.materials(p["xs"], p["ys"], p["zs"], geom, p["props"])
+    oV = o.block_offsets(p["xs"], p["ys"], p["zs"])[3]
+    for (xr_n, (counter, xr, Hr)), (x, H, st) in zip(enumerate(ref), got):
+        assert st["status"] == 0
+        assert rel_l2(x[:oV], xr[:oV]) <= 1e-8, (counter, rel_l2(x[:oV], xr[:oV]))
+        for q in range(3):
+            assert rel_l2(H[q], Hr[q]) <= 1e-8, (counter, q)
+        jv = o.edge_current_from_v(p["xs"], p["ys"], p["zs"], p["dx"], p["dy"], p["dz"], c, x)
+        jr = o.edge_current_from_v(p["xs"], p["ys"], p["zs"], p["dx"], p["dy"], p["dz"], c, xr)
+        if np.linalg.norm(jr) > 0:
+            assert rel_l2(jv, jr) <= 1e-8, (counter, rel_l2(jv, jr))
+
+
+def test_bad_material_id_rejected():
+    from alpineqms_gb300._lib import QMSError
+    xs = ys = zs = 6
+    geom = np.zeros(xs * ys * zs)
+    geom[5] = 7.0
+    props = np.array([[1, 1, 1, 1, 0, 0, 0]], np.float64)
+    from alpineqms_gb300.solver import QMSSolver, default_desc
+    with QMSSolver(default_desc(xs, ys, zs, 1e-3, 1e-3, 1e-3, 1e-5)) as s:
+        with pytest.raises(QMSError):
+            s.set_geometry_f64(geom, props)
