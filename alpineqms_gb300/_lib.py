@@ -31,7 +31,13 @@ class QmsDesc(ctypes.Structure):
                 ("max_inner", ctypes.c_int),
                 ("inner_rtol", ctypes.c_double),
                 ("check_every", ctypes.c_int),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int),
+                ("precond", ctypes.c_int),
+                ("mg_sweeps", ctypes.c_int),
+                ("mg_omega", ctypes.c_double),
+                ("mg_vshift", ctypes.c_double),
+                ("krylov", ctypes.c_int),
+                ("gmres_m", ctypes.c_int)]
 
 
 class QmsStats(ctypes.Structure):
@@ -45,7 +51,8 @@ class QmsStats(ctypes.Structure):
 class QmsProfile(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64),
                 ("op32_launches", ctypes.c_int64), ("op32_ms", ctypes.c_double), ("op32_bytes", ctypes.c_double),
-                ("op64_launches", ctypes.c_int64), ("op64_ms", ctypes.c_double), ("op64_bytes", ctypes.c_double)]
+                ("op64_launches", ctypes.c_int64), ("op64_ms", ctypes.c_double), ("op64_bytes", ctypes.c_double),
+                ("mg_cycles", ctypes.c_int64), ("mg_ms", ctypes.c_double)]
 
 
 QMS_PREC_MIXED, QMS_PREC_FP64 = 0, 1

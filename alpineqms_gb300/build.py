@@ -24,6 +24,7 @@ SOURCES = {
     "qms_exact.cu": ["-fmad=false"],
     "qms_operator.cu": [],
     "qms_solver.cu": [],
+    "qms_mg.cu": [],
     "qms_capi.cu": [],
 }
 

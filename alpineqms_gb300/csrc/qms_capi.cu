@@ -37,10 +37,16 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->precision = QMS_PREC_MIXED;
     d->tol = 1e-12;
     d->max_outer = 30;
-    d->max_inner = 2000;
+    d->max_inner = 500;
     d->inner_rtol = 1e-3;
-    d->check_every = 10;
+    d->check_every = 2;
     d->device = 0;
+    d->precond = QMS_PRECOND_MG;
+    d->mg_sweeps = 2;
+    d->mg_omega = 0.8;
+    d->mg_vshift = 0.0;
+    d->krylov = QMS_KRYLOV_GMRES;
+    d->gmres_m = 24;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }

@@ -1,0 +1,51 @@
+// qms_mg.h -- block-diagonal aggregation multigrid (see qms_mg.cu).
+#pragma once
+#include "qms_internal.h"
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#define MG_MAX_BLOCKS 4
+
+struct MGBlockDesc {
+    int n1, n2, n3;
+    long long off;          // first point of this block in the level's flat arrays
+};
+
+// one level of the hierarchy: all blocks back to back (a packed descriptor table)
+template <typename T>
+struct MGLevelDev {
+    int nb;
+    MGBlockDesc blk[MG_MAX_BLOCKS];
+    long long total;
+    T* w1;                  // link to the +1 neighbour along axis 1 (0 when absent / inactive)
+    T* w2;
+    T* w3;
+    T* dg;                  // diagonal
+    T* dinv;                // 1/diagonal, 0 on inactive (Dirichlet) points
+    T* x;                   // correction (levels > 0)
+    T* b;                   // right-hand side (levels > 0)
+    T* t;                   // Jacobi temporary
+};
+
+template <typename T>
+struct QmsMG {
+    std::vector<MGLevelDev<T>> lv;
+    double* dminv = nullptr;       // dense FP64 inverses of the coarsest blocks
+    long long* dmoff = nullptr;
+    int nu1 = 2, nu2 = 2;
+    T omega = T(0.8);
+    T alpha = T(1);
+    int min_coarse = 5;
+    int max_levels = 12;
+    T* cur_x0 = nullptr;
+    T* cur_t0 = nullptr;
+    std::string err;
+
+    ~QmsMG();
+    void release();
+    static size_t bytes_for(const QGrid& g, int min_coarse);
+    int build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T vshift, cudaStream_t st);
+    int vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v, cudaStream_t st);
+};

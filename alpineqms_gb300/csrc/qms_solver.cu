@@ -145,14 +145,14 @@ __global__ void qk_bicg_s(long long n, const T* __restrict__ r, const T* __restr
 }
 
 template <typename T>
-__global__ void qk_bicg_xr(long long n, const T* __restrict__ p, const T* __restrict__ s, const T* __restrict__ tt,
-                           const T* __restrict__ rh, T* __restrict__ e, T* __restrict__ r, const double* __restrict__ S,
-                           double* __restrict__ part) {
+__global__ void qk_bicg_xr(long long n, const T* __restrict__ y, const T* __restrict__ z, const T* __restrict__ s,
+                           const T* __restrict__ tt, const T* __restrict__ rh, T* __restrict__ e, T* __restrict__ r,
+                           const double* __restrict__ S, double* __restrict__ part) {
     const T al = (T)S[S_ALPHA], om = (T)S[S_OMEGA];
     float a0 = 0.f, a1 = 0.f;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         T st = s[t];
-        e[t] += al * p[t] + om * st;
+        e[t] += al * y[t] + om * z[t];
         T rn = st - om * tt[t];
         r[t] = rn;
         a0 += (float)(rh[t] * rn);
@@ -161,40 +161,47 @@ __global__ void qk_bicg_xr(long long n, const T* __restrict__ p, const T* __rest
     store_partials<T>(part, a0, a1);
 }
 
+// r = D (D^-1 r64) / ||.||  (unscaled residual of the normalised system), e = 0
 template <typename T>
-__global__ void qk_cg_init(long long n, long long mask_from, const double* __restrict__ r64,
-                           const float* __restrict__ dg, const double* __restrict__ S, T* __restrict__ r,
-                           T* __restrict__ z, T* __restrict__ p, T* __restrict__ e, double* __restrict__ part) {
+__global__ void qk_cg_init(long long n, const double* __restrict__ r64, const float* __restrict__ dg,
+                           const double* __restrict__ S, T* __restrict__ r, T* __restrict__ e) {
     const double inv = S[S_INVNRM];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        r[t] = (T)dg[t] * (T)(r64[t] * inv);
+        e[t] = T(0);
+    }
+}
+
+// Jacobi preconditioner of the unscaled system (V block frozen when mask_from < n)
+template <typename T>
+__global__ void qk_jacobi(long long n, long long mask_from, const T* __restrict__ r, const float* __restrict__ dg,
+                          T* __restrict__ z) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        z[t] = t < mask_from ? r[t] / (T)dg[t] : T(0);
+}
+
+// partials of r.z and z.z; optionally p = z (first iteration)
+template <typename T>
+__global__ void qk_cg_dot(long long n, const T* __restrict__ r, const T* __restrict__ z, T* __restrict__ p,
+                          double* __restrict__ part) {
     float a0 = 0.f, a1 = 0.f;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        T d = (T)dg[t];
-        T rs = (T)(r64[t] * inv);           // scaled residual D^-1 r
-        T rv = d * rs;                      // unscaled residual
-        T zv = t < mask_from ? rs : T(0);   // Jacobi: z = D^-1 r
-        r[t] = rv; z[t] = zv; p[t] = zv; e[t] = T(0);
-        a0 += (float)(rv * zv);
-        a1 += (float)(rs * rs);
+        T zv = z[t];
+        if (p) p[t] = zv;
+        a0 += (float)(r[t] * zv);
+        a1 += (float)(zv * zv);
     }
     store_partials<T>(part, a0, a1);
 }
 
 template <typename T>
-__global__ void qk_cg_update(long long n, long long mask_from, const T* __restrict__ p, const T* __restrict__ q,
-                             const float* __restrict__ dg, const double* __restrict__ S, T* __restrict__ e,
-                             T* __restrict__ r, T* __restrict__ z, double* __restrict__ part) {
+__global__ void qk_cg_update(long long n, const T* __restrict__ p, const T* __restrict__ q,
+                             const double* __restrict__ S, T* __restrict__ e, T* __restrict__ r) {
     const T al = (T)S[S_ALPHA];
-    float a0 = 0.f, a1 = 0.f;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         e[t] += al * p[t];
-        T rv = r[t] - al * q[t];
-        r[t] = rv;
-        T zv = t < mask_from ? rv / (T)dg[t] : T(0);
-        z[t] = zv;
-        a0 += (float)(rv * zv);
-        a1 += (float)(zv * zv);
+        r[t] -= al * q[t];
     }
-    store_partials<T>(part, a0, a1);
 }
 
 template <typename T>
@@ -209,6 +216,174 @@ __global__ void qk_ir_update(long long n, const T* __restrict__ e, const double*
     const double nr = S[S_NRM];
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
         x[t] += nr * (double)e[t];
+}
+
+
+// --------------------------------------------------------------------------
+// FGMRES (right preconditioned, restarted by the outer refinement) with the
+// Hessenberg matrix, Givens rotations and the residual estimate on the device.
+// --------------------------------------------------------------------------
+#define GM_MAXM 32
+struct GmPtrs { const void* p[GM_MAXM + 1]; };
+
+// block partials of V_i . w for i = 0..j (classical Gram-Schmidt projections)
+template <typename T>
+__global__ void qk_gm_dots(long long n, int j, GmPtrs V, const T* __restrict__ w, double* __restrict__ part) {
+    float acc[GM_MAXM];
+#pragma unroll
+    for (int i = 0; i < GM_MAXM; i++) acc[i] = 0.f;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const float wv = (float)w[t];
+#pragma unroll
+        for (int i = 0; i < GM_MAXM; i++)
+            if (i <= j) acc[i] += (float)((const T*)V.p[i])[t] * wv;
+    }
+    __shared__ double sh[32];
+    for (int i = 0; i <= j; i++) {
+        float a = 0.f;
+#pragma unroll
+        for (int q = 0; q < GM_MAXM; q++) if (q == i) a = acc[q];
+        double sum = qBlockSum(a, sh);
+        if (threadIdx.x == 0) part[(long long)i * gridDim.x + blockIdx.x] = sum;
+    }
+}
+
+// column j of H from the partials (h_ij = V_i . w)
+__global__ void qk_gm_hcol(const double* __restrict__ part, long long nb, int j, int m, double* __restrict__ Hm) {
+    __shared__ double sh[32];
+    for (int i = 0; i <= j; i++) {
+        double acc = 0.0;
+        for (long long t = threadIdx.x; t < nb; t += blockDim.x) acc += part[(long long)i * nb + t];
+        double s = qBlockSum(acc, sh);
+        if (threadIdx.x == 0) Hm[i * m + j] = s;
+    }
+}
+
+// w -= sum_i h_ij V_i ; partials of |w|^2
+template <typename T>
+__global__ void qk_gm_orth(long long n, int j, int m, GmPtrs V, const double* __restrict__ Hm, T* __restrict__ w,
+                           double* __restrict__ part) {
+    T h[GM_MAXM];
+#pragma unroll
+    for (int i = 0; i < GM_MAXM; i++) h[i] = i <= j ? (T)Hm[i * m + j] : T(0);
+    float acc = 0.f;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        T wv = w[t];
+#pragma unroll
+        for (int i = 0; i < GM_MAXM; i++)
+            if (i <= j) wv -= h[i] * ((const T*)V.p[i])[t];
+        w[t] = wv;
+        acc += (float)(wv * wv);
+    }
+    __shared__ double sh[32];
+    double s0 = qBlockSum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s0;
+}
+
+// h_{j+1,j} = |w|, Givens rotations, residual estimate; Gm layout:
+// [0]: beta, [1]: |g_{j+1}|, [2]: 1/h_{j+1,j}, cs[m] at 8, sn[m] at 8+m, g[m+1] at 8+2m
+__global__ void qk_gm_givens(const double* __restrict__ part, long long nb, int j, int m, double* __restrict__ Hm,
+                             double* __restrict__ Gm, unsigned* __restrict__ status) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (long long t = threadIdx.x; t < nb; t += blockDim.x) acc += part[t];
+    double nw = qBlockSum(acc, sh);
+    if (threadIdx.x != 0) return;
+    double hn = sqrt(nw);
+    double* cs = Gm + 8;
+    double* sn = Gm + 8 + m;
+    double* gv = Gm + 8 + 2 * m;
+    Gm[2] = hn > 0.0 ? 1.0 / hn : 0.0;
+    for (int i = 0; i < j; i++) {                // previous rotations on column j
+        double a = Hm[i * m + j], b = Hm[(i + 1) * m + j];
+        Hm[i * m + j] = cs[i] * a + sn[i] * b;
+        Hm[(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+    }
+    double a = Hm[j * m + j], b = hn;
+    double r = sqrt(a * a + b * b);
+    double c = r > 0.0 ? a / r : 1.0, s = r > 0.0 ? b / r : 0.0;
+    cs[j] = c; sn[j] = s;
+    Hm[j * m + j] = r;
+    gv[j + 1] = -s * gv[j];
+    gv[j] = c * gv[j];
+    Gm[1] = fabs(gv[j + 1]);
+    if (!(r > 0.0) || !isfinite(r)) atomicOr(status, (unsigned)QMS_ST_BREAKDOWN);
+}
+
+// V_{j+1} = w / h_{j+1,j}
+template <typename T>
+__global__ void qk_gm_scale(long long n, const T* __restrict__ w, T* __restrict__ vout, const double* __restrict__ Gm) {
+    const T inv = (T)Gm[2];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        vout[t] = w[t] * inv;
+}
+
+// v0 = r64 / ||r64|| and g = (beta, 0, ...)
+template <typename T>
+__global__ void qk_gm_init(long long n, const double* __restrict__ r64, const double* __restrict__ S, T* __restrict__ v0) {
+    const double inv = S[S_INVNRM];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        v0[t] = (T)(r64[t] * inv);
+}
+
+__global__ void qk_gm_reset(int m, double* __restrict__ Gm) {
+    for (int q = threadIdx.x; q < 8 + 3 * m + 1; q += blockDim.x) Gm[q] = 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0) { Gm[0] = 1.0; Gm[8 + 2 * m] = 1.0; Gm[1] = 1.0; }
+}
+
+// back substitution H(0:k,0:k) y = g(0:k); y stored at Gm + 8 + 3m + 1
+__global__ void qk_gm_solve(int k, int m, const double* __restrict__ Hm, double* __restrict__ Gm) {
+    if (threadIdx.x != 0) return;
+    const double* gv = Gm + 8 + 2 * m;
+    double* y = Gm + 8 + 3 * m + 1;
+    for (int i = k - 1; i >= 0; i--) {
+        double acc = gv[i];
+        for (int q = i + 1; q < k; q++) acc -= Hm[i * m + q] * y[q];
+        const double d = Hm[i * m + i];
+        y[i] = d != 0.0 ? acc / d : 0.0;
+    }
+}
+
+// x += ||r|| * sum_i y_i Z_i   (FP64 accumulation of the refinement)
+template <typename T>
+__global__ void qk_gm_update(long long n, int k, int m, GmPtrs Z, const double* __restrict__ Gm,
+                             const double* __restrict__ S, double* __restrict__ x) {
+    const double* yv = Gm + 8 + 3 * m + 1;
+    T y[GM_MAXM];
+#pragma unroll
+    for (int i = 0; i < GM_MAXM; i++) y[i] = i < k ? (T)yv[i] : T(0);
+    const double nr = S[S_NRM];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        T acc = T(0);
+#pragma unroll
+        for (int i = 0; i < GM_MAXM; i++)
+            if (i < k) acc += y[i] * ((const T*)Z.p[i])[t];
+        x[t] += nr * (double)acc;
+    }
+}
+
+// x -= ||r_prev|| * e  (undo a refinement correction that increased the residual)
+template <typename T>
+__global__ void qk_ir_revert_gm(long long n, int k, int m, GmPtrs Z, const double* __restrict__ Gm, double nrm,
+                                double* __restrict__ x) {
+    const double* yv = Gm + 8 + 3 * m + 1;
+    T y[GM_MAXM];
+#pragma unroll
+    for (int i = 0; i < GM_MAXM; i++) y[i] = i < k ? (T)yv[i] : T(0);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        T acc = T(0);
+#pragma unroll
+        for (int i = 0; i < GM_MAXM; i++)
+            if (i < k) acc += y[i] * ((const T*)Z.p[i])[t];
+        x[t] -= nrm * (double)acc;
+    }
+}
+
+template <typename T>
+__global__ void qk_ir_revert(long long n, const T* __restrict__ e, double nrm, double* __restrict__ x) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        x[t] -= nrm * (double)e[t];
 }
 
 // --------------------------------------------------------------------------
@@ -248,7 +423,13 @@ QmsSolver::~QmsSolver() { release(); }
 
 void QmsSolver::release() {
     if (dev >= 0) cudaSetDevice(dev);
-    void* ptrs[] = {ids, dtab64, dtab32, x, b, r64, H, slicebuf, part, S, status, dg_steady, dg_tr};
+    mgf[0].release(); mgf[1].release(); mgd[0].release(); mgd[1].release();
+    for (auto& p : gmV) { if (p) cudaFree(p); p = nullptr; }
+    for (auto& p : gmZ) { if (p) cudaFree(p); p = nullptr; }
+    if (gm_H) cudaFree(gm_H);
+    if (gm_scal) cudaFree(gm_scal);
+    gm_H = gm_scal = nullptr;
+    void* ptrs[] = {ids, dtab64, dtab32, x, b, r64, H, slicebuf, part, S, status, dg_steady, dg_tr, mgtmp};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -256,7 +437,7 @@ void QmsSolver::release() {
     evpool.clear();
     if (st && own_stream) cudaStreamDestroy(st);
     ids = nullptr; dtab64 = nullptr; dtab32 = nullptr; x = b = r64 = H = slicebuf = part = S = nullptr;
-    status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr;
+    status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr;
     for (auto& p : vec) p = nullptr;
 }
 
@@ -275,7 +456,7 @@ int QmsSolver::init(const qms_desc& d) {
     long long need = (g.n + 255) / 256;
     if (need < vec_blocks) vec_blocks = need;
     nbop = qms_op_num_blocks(g);
-    long long npart = std::max(4 * nbop, 2 * vec_blocks) + 64;
+    long long npart = std::max(4 * nbop, (long long)(GM_MAXM + 1) * vec_blocks) + 64;
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     own_stream = true;
     const long long n = g.n, ncell = (long long)g.xs * g.ys * g.zs;
@@ -297,6 +478,16 @@ int QmsSolver::init(const qms_desc& d) {
     CK(cudaMalloc(&dg_steady, n * 4));
     CK(cudaMalloc(&dg_tr, n * 4));
     for (auto& p : vec) CK(cudaMalloc(&p, n * tsize));
+    use_mg = d.precond == QMS_PRECOND_MG;
+    CK(cudaMalloc(&mgtmp, n * tsize));
+    if (d.krylov == QMS_KRYLOV_GMRES) {
+        const int m = std::min(std::max(d.gmres_m, 1), GM_MAXM);
+        desc.gmres_m = m;
+        for (int i = 0; i <= m; i++) CK(cudaMalloc(&gmV[i], n * tsize));
+        if (use_mg) for (int i = 0; i < m; i++) CK(cudaMalloc(&gmZ[i], n * tsize));
+        CK(cudaMalloc(&gm_H, (size_t)m * (m + 1) * 8));
+        CK(cudaMalloc(&gm_scal, (size_t)(8 + 4 * m + 8) * 8));
+    }
     CK(cudaMallocHost(&hS, S_COUNT * 8));
     CK(cudaMemset(x, 0, n * 8));
     double vac[6] = {1, 1, 1, 0, 0, 0};
@@ -310,7 +501,9 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
     return ncell + sizeof(QMatTable<double>) + sizeof(QMatTable<float>) + 3 * g.n * 8 + 3 * ncell * 8 +
-           3 * smax * 8 + (4 * nb + 64) * 8 + 2 * g.n * 4 + QMS_NVEC * g.n * ts + 4096;
+           3 * smax * 8 + (4 * nb + 64) * 8 + 2 * g.n * 4 + (QMS_NVEC + 1) * g.n * ts + 4096 +
+           (d.krylov == QMS_KRYLOV_GMRES ? (size_t)(2 * d.gmres_m + 1) * g.n * ts : 0) +
+           (d.precond == QMS_PRECOND_MG ? 2 * (ts == 8 ? QmsMG<double>::bytes_for(g, 5) : QmsMG<float>::bytes_for(g, 5)) : 0);
 }
 
 int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int nmat) {
@@ -331,6 +524,23 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     qms_launch_diag(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
     qms_launch_diag(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
     CK(cudaGetLastError());
+    if (use_mg) {
+        const double vshift = desc.mg_vshift;
+        for (int tr = 0; tr < 2; tr++) {
+            int rc;
+            if (fp64_inner) {
+                QmsMG<double>& M = mgd[tr];
+                M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = desc.mg_omega;
+                rc = M.build(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, tr == 1), vshift, st);
+                if (rc) { err = M.err; return QMS_ERR_CUDA; }
+            } else {
+                QmsMG<float>& M = mgf[tr];
+                M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = (float)desc.mg_omega;
+                rc = M.build(g, coef32(), qms_step_par<float>(g, 0, 0, 0, desc.dt, tr == 1), (float)vshift, st);
+                if (rc) { err = M.err; return QMS_ERR_CUDA; }
+            }
+        }
+    }
     CK(cudaStreamSynchronize(st));
     return 0;
 }
@@ -347,20 +557,9 @@ int QmsSolver::finalize(int fop, int nsum, long long nb) {
 template <typename T>
 void QmsSolver::op(bool adv, int mode, const QStepPar<T>& P, const T* xin, const T* bin, T* y, const T* w,
                    double* partials) {
-    OpEv* ev = nullptr;
-    if (prof) {
-        if (evused == evpool.size()) {
-            OpEv e{};
-            cudaEventCreate(&e.a);
-            cudaEventCreate(&e.b);
-            evpool.push_back(e);
-        }
-        ev = &evpool[evused++];
-        ev->fp64 = sizeof(T) == 8;
-        const double ncell = (double)g.xs * g.ys * g.zs;
-        ev->bytes = (double)g.n * sizeof(T) * (2 + (w && w != xin ? 1 : 0) + (bin ? 1 : 0)) + ncell;
-        cudaEventRecord(ev->a, st);
-    }
+    const double ncell = (double)g.xs * g.ys * g.zs;
+    OpEv* ev = prof_begin(sizeof(T) == 8 ? 1 : 0,
+                          (double)g.n * sizeof(T) * (2 + (w && w != xin ? 1 : 0) + (bin ? 1 : 0)) + ncell);
     qms_launch_operator<T>(g, coef<T>(), P, adv, mode, xin, bin, y, w, partials, st);
     nlaunch++;
     if (ev) cudaEventRecord(ev->b, st);
@@ -369,6 +568,21 @@ template void QmsSolver::op<float>(bool, int, const QStepPar<float>&, const floa
                                    const float*, double*);
 template void QmsSolver::op<double>(bool, int, const QStepPar<double>&, const double*, const double*, double*,
                                     const double*, double*);
+
+QmsSolver::OpEv* QmsSolver::prof_begin(int kind, double bytes) {
+    if (!prof) return nullptr;
+    if (evused == evpool.size()) {
+        OpEv e{};
+        cudaEventCreate(&e.a);
+        cudaEventCreate(&e.b);
+        evpool.push_back(e);
+    }
+    OpEv* ev = &evpool[evused++];
+    ev->kind = kind;
+    ev->bytes = bytes;
+    cudaEventRecord(ev->a, st);
+    return ev;
+}
 
 int QmsSolver::profile_enable(bool on) {
     if (prof || on) {
@@ -386,8 +600,9 @@ int QmsSolver::profile_collect(qms_profile* out) {
     for (size_t q = 0; q < evused; q++) {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, evpool[q].a, evpool[q].b));
-        if (evpool[q].fp64) { profacc.op64_launches++; profacc.op64_ms += ms; profacc.op64_bytes += evpool[q].bytes; }
-        else { profacc.op32_launches++; profacc.op32_ms += ms; profacc.op32_bytes += evpool[q].bytes; }
+        if (evpool[q].kind == 1) { profacc.op64_launches++; profacc.op64_ms += ms; profacc.op64_bytes += evpool[q].bytes; }
+        else if (evpool[q].kind == 0) { profacc.op32_launches++; profacc.op32_ms += ms; profacc.op32_bytes += evpool[q].bytes; }
+        else { profacc.mg_cycles++; profacc.mg_ms += ms; }
     }
     evused = 0;
     profacc.launches = nlaunch;
@@ -402,10 +617,29 @@ int QmsSolver::read_scalars() {
 }
 
 template <typename T>
+void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool transient, bool jacobi_pcg) {
+    if (use_mg) {
+        OpEv* ev = prof_begin(2, 0.0);
+        if (sizeof(T) == 4)
+            nlaunch += mgf[transient ? 1 : 0].vcycle((const float*)r, bscale, (float*)z, (float*)mgtmp, mask_v, st);
+        else
+            nlaunch += mgd[transient ? 1 : 0].vcycle((const double*)r, bscale, (double*)z, (double*)mgtmp, mask_v, st);
+        if (ev) cudaEventRecord(ev->b, st);
+    } else if (jacobi_pcg) {
+        qk_jacobi<T><<<(int)vec_blocks, 256, 0, st>>>(g.n, mask_v ? g.oV : g.n, r, transient ? dg_tr : dg_steady, z);
+        nlaunch++;
+    }
+}
+
+template <typename T>
 int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& iters) {
     const long long n = g.n;
     T* r = (T*)vec[0]; T* rh = (T*)vec[1]; T* p = (T*)vec[2]; T* vv = (T*)vec[3];
     T* s = (T*)vec[4]; T* t = (T*)vec[5]; T* e = (T*)vec[6];
+    // right preconditioner of the row-scaled operator D^-1 M: y = MG(D p); identity without MG
+    T* y = use_mg ? (T*)vec[7] : p;
+    T* z = use_mg ? (T*)vec[8] : s;
+    const float* dg = transient ? dg_tr : dg_steady;
     QStepPar<T> P = qms_step_par<T>(g, v[0], v[1], v[2], desc.dt, transient);
     const int vb = (int)vec_blocks;
     qk_bicg_init<T><<<vb, 256, 0, st>>>(n, r64, S, r, rh, p, vv, e, part);
@@ -416,13 +650,15 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
     for (int it = 0; it < desc.max_inner; it++) {
         qk_bicg_p<T><<<vb, 256, 0, st>>>(n, r, p, vv, S);
         nlaunch++;
-        op<T>(adv, QOPH_SCALED, P, p, nullptr, vv, rh, part);
+        if (use_mg) precond<T>(p, dg, y, false, transient, false);
+        op<T>(adv, QOPH_SCALED, P, y, nullptr, vv, rh, part);
         finalize(FIN_BICG_ALPHA, 1, nbop);
         qk_bicg_s<T><<<vb, 256, 0, st>>>(n, r, vv, s, S);
         nlaunch++;
-        op<T>(adv, QOPH_SCALED, P, s, nullptr, t, s, part);
+        if (use_mg) precond<T>(s, dg, z, false, transient, false);
+        op<T>(adv, QOPH_SCALED, P, z, nullptr, t, s, part);
         finalize(FIN_BICG_OMEGA, 2, nbop);
-        qk_bicg_xr<T><<<vb, 256, 0, st>>>(n, p, s, t, rh, e, r, S, part);
+        qk_bicg_xr<T><<<vb, 256, 0, st>>>(n, y, z, s, t, rh, e, r, S, part);
         nlaunch++;
         finalize(FIN_BICG_RHO, 2, vec_blocks);
         iters = it + 1;
@@ -444,6 +680,64 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
     return 0;
 }
 
+
+template <typename T>
+int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& iters) {
+    const long long n = g.n;
+    const int m = std::min(desc.gmres_m, GM_MAXM);
+    const float* dg = transient ? dg_tr : dg_steady;
+    QStepPar<T> P = qms_step_par<T>(g, v[0], v[1], v[2], desc.dt, transient);
+    const int vb = (int)vec_blocks;
+    GmPtrs Vp{}, Zp{};
+    for (int i = 0; i <= m; i++) Vp.p[i] = gmV[i];
+    for (int i = 0; i < m; i++) Zp.p[i] = use_mg ? gmZ[i] : gmV[i];
+    T* w = (T*)vec[0];
+    qk_gm_reset<<<1, 128, 0, st>>>(m, gm_scal);
+    qk_gm_init<T><<<vb, 256, 0, st>>>(n, r64, S, (T*)gmV[0]);
+    nlaunch += 2;
+    const double tol = desc.inner_rtol;
+    int k = 0;
+    for (int j = 0; j < m; j++) {
+        T* vj = (T*)gmV[j];
+        T* zj = use_mg ? (T*)gmZ[j] : vj;
+        if (use_mg) precond<T>(vj, dg, zj, false, transient, false);
+        op<T>(adv, QOPH_SCALED, P, zj, nullptr, w, nullptr, nullptr);
+        qk_gm_dots<T><<<vb, 256, 0, st>>>(n, j, Vp, w, part);
+        qk_gm_hcol<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H);
+        qk_gm_orth<T><<<vb, 256, 0, st>>>(n, j, m, Vp, gm_H, w, part);
+        qk_gm_givens<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H, gm_scal, status);
+        qk_gm_scale<T><<<vb, 256, 0, st>>>(n, w, (T*)gmV[j + 1], gm_scal);
+        nlaunch += 5;
+        k = j + 1;
+        if ((j + 1) % desc.check_every == 0 || j + 1 == m) {
+            CK(cudaMemcpyAsync(hS, gm_scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (!(hS[1] > tol * hS[0])) break;       // also stops on a non-finite estimate
+        }
+    }
+    qk_gm_solve<<<1, 32, 0, st>>>(k, m, gm_H, gm_scal);
+    qk_gm_update<T><<<vb, 256, 0, st>>>(n, k, m, Zp, gm_scal, S, x);
+    nlaunch += 2;
+    last_gm_k = k;
+    iters = k;
+    CK(cudaGetLastError());
+    return 0;
+}
+
+template <typename T>
+void QmsSolver::revert_last(double nrm) {
+    const int vb = (int)vec_blocks;
+    if (last_inner == 2) {
+        const int m = std::min(desc.gmres_m, GM_MAXM);
+        GmPtrs Zp{};
+        for (int i = 0; i < m; i++) Zp.p[i] = use_mg ? gmZ[i] : gmV[i];
+        qk_ir_revert_gm<T><<<vb, 256, 0, st>>>(g.n, last_gm_k, m, Zp, gm_scal, nrm, x);
+    } else {
+        qk_ir_revert<T><<<vb, 256, 0, st>>>(g.n, (const T*)vec[6], nrm, x);
+    }
+    nlaunch++;
+}
+
 template <typename T>
 int QmsSolver::inner_pcg(bool transient, int& iters) {
     const long long n = g.n;
@@ -451,8 +745,11 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
     const float* dg = transient ? dg_tr : dg_steady;
     QStepPar<T> P = qms_step_par<T>(g, 0, 0, 0, desc.dt, transient);
     const int vb = (int)vec_blocks;
-    const long long mask_from = g.oV;     // V block frozen at zero (steady, v = 0)
-    qk_cg_init<T><<<vb, 256, 0, st>>>(n, mask_from, r64, dg, S, r, z, p, e, part);
+    // V block frozen at zero: the steady magnetostatic system with v = 0 has V = 0
+    qk_cg_init<T><<<vb, 256, 0, st>>>(n, r64, dg, S, r, e);
+    nlaunch++;
+    precond<T>(r, nullptr, z, true, transient, true);
+    qk_cg_dot<T><<<vb, 256, 0, st>>>(n, r, z, p, part);
     nlaunch++;
     finalize(FIN_CG_INIT, 2, vec_blocks);
     const double tol2 = desc.inner_rtol * desc.inner_rtol;
@@ -460,7 +757,10 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
     for (int it = 0; it < desc.max_inner; it++) {
         op<T>(false, QOPH_APPLY, P, p, nullptr, q, p, part);
         finalize(FIN_CG_ALPHA, 1, nbop);
-        qk_cg_update<T><<<vb, 256, 0, st>>>(n, mask_from, p, q, dg, S, e, r, z, part);
+        qk_cg_update<T><<<vb, 256, 0, st>>>(n, p, q, S, e, r);
+        nlaunch++;
+        precond<T>(r, nullptr, z, true, transient, true);
+        qk_cg_dot<T><<<vb, 256, 0, st>>>(n, r, z, (T*)nullptr, part);
         nlaunch++;
         finalize(FIN_CG_BETA, 2, vec_blocks);
         iters = it + 1;
@@ -498,22 +798,51 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     const bool adv = v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
     const bool use_cg = !transient && !adv;
     stats = qms_stats{};
-    double rel = INFINITY;
-    int outer = 0;
+    double rel = INFINITY, prev_rn = INFINITY, sref = 0.0;
+    int outer = 0, stalled = 0;
     for (;;) {
         int rc = residual(adv, transient, v);
         if (rc) return rc;
-        double xn = std::sqrt(hS[S_XA] + hS[S_XV]);
-        double rn = std::sqrt(hS[S_RA] + hS[S_RV]);
-        rel = xn > 0 ? rn / xn : rn;
+        const double xn = std::sqrt(hS[S_XA] + hS[S_XV]);
+        const double rn = std::sqrt(hS[S_RA] + hS[S_RV]);
+        // The scale is fixed by the state at the start of the solve (the previous step, or the
+        // Dirichlet values for the steady state): a correction that blew up x must not make
+        // ||r|| / ||x|| look small.
+        if (outer == 0) sref = xn > 0 ? xn : 1.0;
+        const double scale = std::min(std::max(xn, sref), 100.0 * sref);
+        rel = rn / scale;
         if (outer == 0) stats.initial_residual = rel;
         if (!std::isfinite(rel)) { stats.status |= QMS_ST_NAN; break; }
         if (rel <= desc.tol || rn == 0.0) break;
+        // refinement at the round-off floor: two iterations without halving the residual
+        stalled = rn > 0.5 * prev_rn ? stalled + 1 : 0;
+        if (stalled >= 2) {
+            if (rel > 1e3 * desc.tol) stats.status |= QMS_ST_NO_CONVERGENCE;
+            break;
+        }
+        if (outer > 0 && rn > prev_rn) {
+            // the last correction increased the residual: undo it and stop at the previous state
+            if (fp64_inner) revert_last<double>(prev_rn); else revert_last<float>(prev_rn);
+            rc = residual(adv, transient, v);
+            if (rc) return rc;
+            rel = std::sqrt(hS[S_RA] + hS[S_RV]) / scale;
+            if (rel > 1e3 * desc.tol) stats.status |= QMS_ST_NO_CONVERGENCE;
+            break;
+        }
         if (outer >= desc.max_outer) { stats.status |= QMS_ST_NO_CONVERGENCE; break; }
+        prev_rn = rn;
         int it = 0;
-        if (use_cg) rc = fp64_inner ? inner_pcg<double>(transient, it) : inner_pcg<float>(transient, it);
-        else rc = fp64_inner ? inner_bicgstab<double>(adv, transient, v, it)
-                             : inner_bicgstab<float>(adv, transient, v, it);
+        if (use_cg) {
+            last_inner = 0;
+            rc = fp64_inner ? inner_pcg<double>(transient, it) : inner_pcg<float>(transient, it);
+        } else if (desc.krylov == QMS_KRYLOV_BICGSTAB) {
+            last_inner = 1;
+            rc = fp64_inner ? inner_bicgstab<double>(adv, transient, v, it)
+                            : inner_bicgstab<float>(adv, transient, v, it);
+        } else {
+            last_inner = 2;
+            rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it) : inner_gmres<float>(adv, transient, v, it);
+        }
         if (rc) return rc;
         stats.inner_iterations += it;
         outer++;
@@ -551,3 +880,9 @@ template int QmsSolver::inner_bicgstab<float>(bool, bool, const double*, int&);
 template int QmsSolver::inner_bicgstab<double>(bool, bool, const double*, int&);
 template int QmsSolver::inner_pcg<float>(bool, int&);
 template int QmsSolver::inner_pcg<double>(bool, int&);
+template int QmsSolver::inner_gmres<float>(bool, bool, const double*, int&);
+template int QmsSolver::inner_gmres<double>(bool, bool, const double*, int&);
+template void QmsSolver::revert_last<float>(double);
+template void QmsSolver::revert_last<double>(double);
+template void QmsSolver::precond<float>(const float*, const float*, float*, bool, bool, bool);
+template void QmsSolver::precond<double>(const double*, const float*, double*, bool, bool, bool);

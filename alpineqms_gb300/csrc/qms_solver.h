@@ -2,12 +2,13 @@
 #pragma once
 #include "qms.h"
 #include "qms_internal.h"
+#include "qms_mg.h"
 
 #include <algorithm>
 #include <string>
 #include <vector>
 
-#define QMS_NVEC 7
+#define QMS_NVEC 9   // r, rh, p, v, s, t, e, y, z  (+ MG level-0 temporary)
 
 size_t qms_device_bytes_impl(const qms_desc& d);
 
@@ -38,6 +39,13 @@ struct QmsSolver {
     float* dg_steady = nullptr; // Jacobi diagonals
     float* dg_tr = nullptr;
     void* vec[QMS_NVEC] = {};   // inner Krylov vectors (FP32 or FP64)
+    float* mgtmp = nullptr;     // level-0 Jacobi temporary of the multigrid
+    QmsMG<float> mgf[2];        // hierarchies of the steady [0] and transient [1] operators (mixed)
+    QmsMG<double> mgd[2];       // the same in FP64 (plain FP64 solver)
+    bool use_mg = false;
+    // z = preconditioner(r): multigrid on (bscale .* r) or the Jacobi / identity fallback
+    template <typename T> void precond(const T* r, const float* bscale, T* z, bool mask_v, bool transient,
+                                       bool jacobi_pcg);
 
     qms_stats stats{};
     std::string err;
@@ -45,7 +53,8 @@ struct QmsSolver {
     // instrumentation (qms_profile_enable)
     bool prof = false;
     long long nlaunch = 0;
-    struct OpEv { cudaEvent_t a, b; int fp64; double bytes; };
+    struct OpEv { cudaEvent_t a, b; int kind; double bytes; };   // kind: 0 op32, 1 op64, 2 V-cycle
+    OpEv* prof_begin(int kind, double bytes);
     std::vector<OpEv> evpool;
     size_t evused = 0;
     qms_profile profacc{};
@@ -70,6 +79,14 @@ struct QmsSolver {
 
     template <typename T> int inner_bicgstab(bool adv, bool transient, const double v[3], int& iters);
     template <typename T> int inner_pcg(bool transient, int& iters);
+    template <typename T> int inner_gmres(bool adv, bool transient, const double v[3], int& iters);
+    template <typename T> void revert_last(double nrm);
+    void* gmV[33] = {};         // FGMRES basis (m + 1) and preconditioned directions (m)
+    void* gmZ[32] = {};
+    double* gm_H = nullptr;     // Hessenberg matrix (m+1) x m, row-major with stride m
+    double* gm_scal = nullptr;  // beta, |g_{j+1}|, 1/h, rotations, g, y
+    int last_gm_k = 0;
+    int last_inner = 0;         // 0 PCG, 1 BiCGSTAB, 2 FGMRES
 };
 
 template <> inline QCoef<float> QmsSolver::coef<float>() const { return coef32(); }

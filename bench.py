@@ -166,7 +166,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    size = args.cpu_size or 32
+    size = args.cpu_size or 20
     steps = args.cpu_steps or max(args.steps, 3)
     for _ in range(max(args.warmup, 0)):
         pass  # the first (refactoring) step inside cpu_sample is the warm-up
@@ -284,12 +284,13 @@ def run_gpu(args):
                 "avg_launch_us": 1e3 * kms / max(klaunch, 1),
                 "algorithmic_bytes_per_launch": kbytes / max(klaunch, 1),
                 "share_of_step": kms / ms if ms > 0 else None,
-                "op32_ms": prof["op32_ms"], "op64_ms": prof["op64_ms"]}
+                "op32_ms": prof["op32_ms"], "op64_ms": prof["op64_ms"], "mg_ms": prof["mg_ms"],
+                "mg_cycles": prof["mg_cycles"]}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_sample(args.cpu_size or 32, args.cpu_steps or 5)
+            cpu = cpu_sample(args.cpu_size or 20, args.cpu_steps or 5)
         except Exception as e:  # the baseline is a report, never the product path
             cpu = {"error": repr(e)}
 

@@ -59,6 +59,8 @@ enum {
 
 enum { QMS_PREC_MIXED = 0, QMS_PREC_FP64 = 1 };
 enum { QMS_FIELD_CUBES = 0, QMS_FIELD_SLICE = 1 };
+enum { QMS_PRECOND_JACOBI = 0, QMS_PRECOND_MG = 1 };
+enum { QMS_KRYLOV_GMRES = 0, QMS_KRYLOV_BICGSTAB = 1 };
 
 /* status bits reported in qms_stats.status */
 enum {
@@ -80,6 +82,14 @@ typedef struct {
     double inner_rtol;       /* relative reduction asked of each inner solve */
     int check_every;         /* inner iterations between host convergence checks */
     int device;              /* CUDA device ordinal */
+    int precond;             /* QMS_PRECOND_MG (default) or QMS_PRECOND_JACOBI */
+    int mg_sweeps;           /* Jacobi sweeps before and after each coarse correction */
+    double mg_omega;         /* Jacobi weight */
+    double mg_vshift;        /* relative diagonal shift of the preconditioner's V block (0 by default:
+                                the coarsest V solve is a pseudo-inverse that drops the floating
+                                potential of isolated conductors) */
+    int krylov;              /* nonsymmetric inner solver: QMS_KRYLOV_GMRES (default) or _BICGSTAB */
+    int gmres_m;             /* FGMRES basis size per refinement iteration (<= 32) */
 } qms_desc;
 
 typedef struct {
@@ -151,6 +161,8 @@ typedef struct {
     int64_t op64_launches;   /* FP64 operator applications (residuals) */
     double op64_ms;
     double op64_bytes;
+    int64_t mg_cycles;       /* multigrid V-cycles */
+    double mg_ms;            /* their summed device time */
 } qms_profile;
 int qms_profile_enable(qms_handle* h, int on);
 int qms_get_profile(qms_handle* h, qms_profile* out);

@@ -208,22 +208,42 @@ class DirectSolver:
     def __init__(self):
         self.lu = None
 
-    def factor(self, ia, ja, a, n):
+    def factor(self, ia, ja, a, n, symmetric_mode=True):
         import scipy.sparse as sp
         import scipy.sparse.linalg as spl
         A = to_scipy(ia, ja, a, n)
         self.A = A
         self.d = np.abs(A.diagonal())
-        self.lu = spl.splu((sp.diags(1.0 / self.d) @ A).tocsc(), permc_spec="COLAMD")
+        As = (sp.diags(1.0 / self.d) @ A).tocsc()
+        if symmetric_mode:
+            # diagonal pivots on the equilibrated matrix with a symmetric (A+A^T) ordering:
+            # far less fill than column ordering with partial pivoting on this system
+            self.lu = spl.splu(As, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0,
+                               options={"SymmetricMode": True})
+        else:
+            self.lu = spl.splu(As, permc_spec="COLAMD")
+        self._As = As
 
     def solve(self, b, max_refine=8):
         b = np.asarray(b, dtype=np.float64)
+        x = self._refine(b, max_refine)
+        if not self._ok(b, x):              # pivoting trouble: fall back to partial pivoting
+            import scipy.sparse.linalg as spl
+            self.lu = spl.splu(self._As, permc_spec="COLAMD")
+            x = self._refine(b, max_refine)
+        return x
+
+    def _ok(self, b, x):
+        r = (b - self.A @ x) / self.d
+        return np.isfinite(r).all() and np.linalg.norm(r) <= 1e-13 * max(np.linalg.norm(x), 1e-300)
+
+    def _refine(self, b, max_refine):
         x = self.lu.solve(b / self.d)
         best = None
         for _ in range(max_refine):
             r = (b - self.A @ x) / self.d
             nr = np.linalg.norm(r)
-            if best is not None and nr >= 0.5 * best:
+            if not np.isfinite(nr) or (best is not None and nr >= 0.5 * best):
                 break
             best = nr if best is None else min(best, nr)
             x = x + self.lu.solve(r)

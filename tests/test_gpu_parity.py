@@ -188,10 +188,11 @@ def _conductor_case(moving):
 
 @pytest.mark.parametrize("moving", [False, True])
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_solve_matches_direct_oracle(moving, precision):
+@pytest.mark.parametrize("precond", [1, 0], ids=["mg", "jacobi"])
+def test_solve_matches_direct_oracle(moving, precision, precond):
     p, geom = _conductor_case(moving)
     ref = o.simulate(p, geom, steps=3, keep_states=True)
-    got = _run_gpu(p, geom, precision, 3)
+    got = _run_gpu(p, geom, precision, 3, precond=precond)
     c = o.materials(p["xs"], p["ys"], p["zs"], geom, p["props"])
     oV = o.block_offsets(p["xs"], p["ys"], p["zs"])[3]
     for (xr_n, (counter, xr, Hr)), (x, H, st) in zip(enumerate(ref), got):
@@ -215,3 +216,29 @@ def test_bad_material_id_rejected():
     with QMSSolver(default_desc(xs, ys, zs, 1e-3, 1e-3, 1e-3, 1e-5)) as s:
         with pytest.raises(QMSError):
             s.set_geometry_f64(geom, props)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_dropin_dumps_vs_reference_program(name, tmp_path):
+    """The drop-in QMS_3D run on each golden case writes the same dump files (record
+    structure identical, values within 1e-8 relative L2 of the reference program's)."""
+    from alpineqms_gb300 import qms3d
+    from alpineqms_gb300.records import read_records
+    z = load_golden(name)
+    (tmp_path / "inputs.txt").write_bytes(bytes(z["inputs_txt"]))
+    z["geom"].astype("<f8").flatten(order="F").tofile(str(tmp_path / "geom.bin"))
+    qms3d.run(str(tmp_path / "inputs.txt"), workdir=str(tmp_path), log=lambda *a: None)
+    for nm in ("Hx.bin", "Hy.bin", "Hz.bin", "Hx_all.bin", "Hy_all.bin", "Hz_all.bin"):
+        key = "dump_" + nm.replace(".", "_")
+        path = tmp_path / nm
+        if key not in z:
+            assert not path.exists(), nm
+            continue
+        got = path.read_bytes()
+        ref_path = tmp_path / ("ref_" + nm)
+        ref_path.write_bytes(bytes(z[key]))
+        assert len(got) == len(bytes(z[key])), nm
+        g_recs, r_recs = read_records(str(path)), read_records(str(ref_path))
+        assert len(g_recs) == len(r_recs)
+        for a, b in zip(g_recs, r_recs):
+            assert rel_l2(a, b, floor=1e-30) <= 1e-8, (nm, rel_l2(a, b))
