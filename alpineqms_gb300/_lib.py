@@ -87,6 +87,9 @@ SIGNATURES = [
     ("qms_profile_enable", ctypes.c_int, [_H, ctypes.c_int]),
     ("qms_get_profile", ctypes.c_int, [_H, ctypes.POINTER(QmsProfile)]),
     ("qms_get_stream", ctypes.c_void_p, [_H]),
+    ("qms_residual_noalloc", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int, _DP, _VP, _VP,
+                                                                                      ctypes.c_int, _VP, _VP, _VP,
+                                                                                      _VP, _VP]),
 ]
 
 

@@ -25,6 +25,7 @@ SOURCES = {
     "qms_operator.cu": [],
     "qms_solver.cu": [],
     "qms_mg.cu": [],
+    "qms_noalloc.cu": [],
     "qms_capi.cu": [],
 }
 

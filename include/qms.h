@@ -169,6 +169,29 @@ int qms_get_profile(qms_handle* h, qms_profile* out);
 /* The cudaStream_t all work of the handle runs on (to record events around calls). */
 void* qms_get_stream(qms_handle* h);
 
+/* Residual check for callers that cannot allocate device memory.  This entry
+ * point has no counterpart in the reference (whose solve is a direct PARDISO
+ * call with no residual output).  It is meant for code that may not call
+ * cudaMalloc -- for example code running inside a CUDA stream capture of its
+ * own, or a process whose device memory is owned by another runtime's pool --
+ * and therefore cannot create a qms_handle.  It computes, on `stream`,
+ *   d_r    = D^-1 (b - M x)                      (n_dims doubles, D = diag M)
+ *   d_sums = |r_A|^2, |r_V|^2, |x_A|^2, |x_V|^2  (4 doubles)
+ * for the steady (transient = 0) or transient operator with frame velocity v,
+ * from caller-owned device buffers: d_slots (xs*ys*zs uint8 material slots,
+ * Fortran order), d_x and d_b (n_dims doubles).  rows: host array of nmat x 6
+ * doubles (mu_r x,y,z, sigma x,y,z).  It allocates nothing: its scratch is a
+ * fixed static device array sized for at most 32768 operator tiles (grids up
+ * to about 512 x 512 x 256 cells, or any grid with
+ * ceil((xs+1)/32) * ceil((ys+1)/8) * ceil((zs+1)/16) <= 32768); larger grids are
+ * rejected with QMS_ERR_ARG.  The first call on a device looks up the scratch
+ * address on that device (make it before any stream capture).  All calls share
+ * the scratch: calls that overlap on the GPU race, so serialise them (the call
+ * returns after synchronising `stream`). */
+int qms_residual_noalloc(int xs, int ys, int zs, double dx, double dy, double dz, double dt, int transient,
+                         const double v[3], const uint8_t* d_slots, const double* rows, int nmat,
+                         const double* d_x, const double* d_b, double* d_r, double* d_sums, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
