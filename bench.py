@@ -181,6 +181,19 @@ def run_reference(args):
     return 0
 
 
+def aggregate_replicas(ms_local, units_local, dist=None, device="cpu"):
+    """Whole-job timing of N independent replicas: the max of the per-rank times and the
+    sum of the units (DOF-timesteps) all ranks processed.  No data-path collective."""
+    if dist is None:
+        return float(ms_local), float(units_local)
+    import torch
+    mx = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    sm = torch.tensor([float(units_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return float(mx.item()), float(sm.item())
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import numpy as np
@@ -234,13 +247,10 @@ def run_gpu(args):
     clk = clocks.stop()
     prof = solver.profile()
     solver.profile_enable(False)
-    ms = ev0.elapsed_time(ev1)
+    ms, units = aggregate_replicas(ev0.elapsed_time(ev1), n * args.steps, dist, "cuda")
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
-    value = world * n * args.steps / (ms / 1e3)
+    value = units / (ms / 1e3)
 
     # end to end through the public API: per step the velocity / field scalars come from
     # pinned host memory and the H slice (what the reference dumps every step) is read back
@@ -262,12 +272,8 @@ def run_gpu(args):
             solver.step(hv[:3], hv[3:6], hv[6:15])
             solver.slices(inp.slice_axis, inp.slice_index)
         torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t1
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 15 * 8,
+        e2e_ms, e2e_units = aggregate_replicas(1e3 * (time.perf_counter() - t1), n * args.steps, dist, "cuda")
+        e2e = {"value": e2e_units / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 15 * 8,
                "d2h_bytes_per_step": slice_bytes}
 
     peak, peak_kind = measured_peak()
