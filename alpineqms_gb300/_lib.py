@@ -37,7 +37,8 @@ class QmsDesc(ctypes.Structure):
                 ("mg_omega", ctypes.c_double),
                 ("mg_vshift", ctypes.c_double),
                 ("krylov", ctypes.c_int),
-                ("gmres_m", ctypes.c_int)]
+                ("gmres_m", ctypes.c_int),
+                ("use_graphs", ctypes.c_int)]
 
 
 class QmsStats(ctypes.Structure):

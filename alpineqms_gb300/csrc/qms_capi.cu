@@ -47,6 +47,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->mg_vshift = 0.0;
     d->krylov = QMS_KRYLOV_GMRES;
     d->gmres_m = 24;
+    d->use_graphs = 1;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }
@@ -62,9 +63,10 @@ int qms_create(const qms_desc* d, qms_handle** out) {
     if (!h) return QMS_ERR_NOMEM;
     qms_desc dd = *d;
     if (dd.check_every <= 0) dd.check_every = 1;
-    if (dd.max_inner <= 0 || dd.max_outer < 0 || !(dd.tol > 0) || !(dd.inner_rtol > 0)) {
+    if (dd.max_inner <= 0 || dd.max_outer < 0 || !(dd.tol > 0) || !(dd.inner_rtol > 0) || dd.mg_sweeps < 1 ||
+        !(dd.mg_omega > 0)) {
         std::lock_guard<std::mutex> lk(g_err_mu);
-        g_create_err = "tol, inner_rtol, max_inner must be positive";
+        g_create_err = "tol, inner_rtol, max_inner, mg_sweeps and mg_omega must be positive";
         delete h;
         return QMS_ERR_ARG;
     }

@@ -93,6 +93,9 @@ struct QCoef {
     const uint8_t* __restrict__ id;
     const QMatTable<T>* __restrict__ tab;
     T imu0;
+    // optional: the six node coefficients (1/mu_x, 1/mu_y, 1/mu_z, sigma_x, sigma_y, sigma_z)
+    // formed once per geometry, structure of arrays of Nn entries each
+    const T* __restrict__ nc = nullptr;
 
     __device__ __forceinline__ int cell(int i, int j, int k) const { return __ldg(id + qCELL(g, i, j, k)); }
     __device__ __forceinline__ bool face(int i, int j, int k) const {

@@ -26,6 +26,8 @@ template <typename T>
 void qms_launch_operator(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, bool adv, int mode, const T* x,
                          const T* b, T* y, const T* w, double* partials, cudaStream_t st);
 void qms_launch_diag(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st);
+template <typename T>
+void qms_launch_node_coef(const QGrid& g, const QCoef<T>& c, T* nc, cudaStream_t st);
 void qms_launch_csr_spmv(long long n, const long long* ia, const int32_t* ja, const double* a, const double* x,
                          double* y, cudaStream_t st);
 

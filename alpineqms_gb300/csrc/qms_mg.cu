@@ -23,7 +23,9 @@
 // back and processed by one launch through a packed block-descriptor table.
 // Smoother: weighted Jacobi.  Coarsest level: dense FP64 inverse per block.
 #include "qms_mg.h"
+#include "qms_tile.cuh"
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -40,18 +42,14 @@ __device__ __forceinline__ int find_block(const MGLevelDev<T>& L, long long t) {
 }
 
 // ---------------------------------------------------------------- fine level
+// links (+1 neighbour along each axis), diagonal and activity of fine point
+// (i, j, k) (1-based) of block b
 template <typename T>
-__global__ void mg_fine_coef(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, MGLevelDev<T> L) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= L.total) return;
-    const int b = find_block(L, t);
-    const MGBlockDesc& B = L.blk[b];
-    long long q = t - B.off;
-    const int i = (int)(q % B.n1) + 1;
-    const int j = (int)((q / B.n1) % B.n2) + 1;
-    const int k = (int)(q / ((long long)B.n1 * B.n2)) + 1;
-    T w1 = 0, w2 = 0, w3 = 0, d = 1;
+__device__ __forceinline__ bool mg_fine_point(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T vshift,
+                                              int b, int i, int j, int k, T& w1, T& w2, T& w3, T& d) {
     bool active;
+    w1 = w2 = w3 = T(0);
+    d = T(1);
     if (b == 0) {            // Ax
         active = !qFixX(g, i, j, k);
         w1 = i < g.xs ? c.imux(i, j, k) * P.idx2 : T(0);
@@ -87,44 +85,64 @@ __global__ void mg_fine_coef(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, MGLev
                  (fmax(c.sgy(i, j, k), fl) + fmax(c.sgy(i, j - 1, k), fl)) * P.idy2 +
                  (fmax(c.sgz(i, j, k), fl) + fmax(c.sgz(i, j, k - 1), fl)) * P.idz2) * (T(1) + vshift);
     }
+    return active;
+}
+
+__device__ __forceinline__ bool mg_fine_active(const QGrid& g, int b, int i, int j, int k) {
+    return b == 0 ? !qFixX(g, i, j, k) : b == 1 ? !qFixY(g, i, j, k) : b == 2 ? !qFixZ(g, i, j, k) : !qFixV(g, i, j, k);
+}
+
+template <typename T>
+__global__ void mg_fine_coef(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, MGLevelDev<T> L) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L.total) return;
+    const int b = find_block(L, t);
+    const MGBlockDesc& B = L.blk[b];
+    long long q = t - B.off;
+    const int i = (int)(q % B.n1) + 1;
+    const int j = (int)((q / B.n1) % B.n2) + 1;
+    const int k = (int)(q / ((long long)B.n1 * B.n2)) + 1;
+    T w1, w2, w3, d;
+    const bool active = mg_fine_point(g, c, P, vshift, b, i, j, k, w1, w2, w3, d);
     L.w1[t] = w1; L.w2[t] = w2; L.w3[t] = w3;
     L.dg[t] = d;                              // diagonal (including links to Dirichlet points)
     L.dinv[t] = active ? T(1) / d : T(0);     // 0 marks an inactive (Dirichlet) point
 }
 
 // -------------------------------------------------------------- coarsening
-// coarse point (I,J,K) aggregates fine points (2I..2I+1, 2J..2J+1, 2K..2K+1) (0-based)
-template <typename T>
-__global__ void mg_coarsen(MGLevelDev<T> F, MGLevelDev<T> C) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= C.total) return;
-    const int b = find_block(C, t);
-    const MGBlockDesc& cb = C.blk[b];
-    const MGBlockDesc& fb = F.blk[b];
+// coarse point (I,J,K) aggregates fine points (2I..2I+1, 2J..2J+1, 2K..2K+1) (0-based):
+// a coarse link is the sum of the fine links crossing between two aggregates, a
+// coarse diagonal the sum of the fine diagonals minus twice the internal links.
+// `fine(b, f, i, j, k, w1, w2, w3, d)` gives fine point f = (i, j, k) of block b and
+// returns whether it is active; `act(b, f, i, j, k)` only its activity.
+template <typename T, typename Fine, typename Act>
+__device__ __forceinline__ void mg_coarsen_point(const MGBlockDesc& fb, const MGBlockDesc& cb, int b, long long t,
+                                                 MGLevelDev<T>& C, Fine fine, Act act) {
     long long q = t - cb.off;
     const int I = (int)(q % cb.n1), J = (int)((q / cb.n1) % cb.n2), K = (int)(q / ((long long)cb.n1 * cb.n2));
     double d = 0.0, w1 = 0.0, w2 = 0.0, w3 = 0.0;
     bool any = false;
-    const long long s1 = 1, s2 = fb.n1, s3 = (long long)fb.n1 * fb.n2;
+    const long long s2 = fb.n1, s3 = (long long)fb.n1 * fb.n2;
     for (int dk = 0; dk < 2; dk++) for (int dj = 0; dj < 2; dj++) for (int di = 0; di < 2; di++) {
         int i = 2 * I + di, j = 2 * J + dj, k = 2 * K + dk;
         if (i >= fb.n1 || j >= fb.n2 || k >= fb.n3) continue;
         long long f = fb.off + i + (long long)j * s2 + (long long)k * s3;
-        if (F.dinv[f] == T(0)) continue;
+        T fw1, fw2, fw3, fd;
+        if (!fine(b, f, i, j, k, fw1, fw2, fw3, fd)) continue;
         any = true;
-        d += F.dg[f];
+        d += fd;
         // +x link of f: internal if di == 0, crossing to I+1 if di == 1
-        if (i + 1 < fb.n1 && F.dinv[f + s1] != T(0)) {
-            if (di == 0) d -= 2.0 * F.w1[f];
-            else w1 += F.w1[f];
+        if (i + 1 < fb.n1 && act(b, f + 1, i + 1, j, k)) {
+            if (di == 0) d -= 2.0 * fw1;
+            else w1 += fw1;
         }
-        if (j + 1 < fb.n2 && F.dinv[f + s2] != T(0)) {
-            if (dj == 0) d -= 2.0 * F.w2[f];
-            else w2 += F.w2[f];
+        if (j + 1 < fb.n2 && act(b, f + s2, i, j + 1, k)) {
+            if (dj == 0) d -= 2.0 * fw2;
+            else w2 += fw2;
         }
-        if (k + 1 < fb.n3 && F.dinv[f + s3] != T(0)) {
-            if (dk == 0) d -= 2.0 * F.w3[f];
-            else w3 += F.w3[f];
+        if (k + 1 < fb.n3 && act(b, f + s3, i, j, k + 1)) {
+            if (dk == 0) d -= 2.0 * fw3;
+            else w3 += fw3;
         }
     }
     C.w1[t] = I + 1 < cb.n1 ? (T)w1 : T(0);
@@ -132,6 +150,33 @@ __global__ void mg_coarsen(MGLevelDev<T> F, MGLevelDev<T> C) {
     C.w3[t] = K + 1 < cb.n3 ? (T)w3 : T(0);
     C.dg[t] = any ? (T)d : T(1);
     C.dinv[t] = any && d > 0.0 ? (T)(1.0 / d) : T(0);
+}
+
+// level l+1 from the stored arrays of level l
+template <typename T>
+__global__ void mg_coarsen(MGLevelDev<T> F, MGLevelDev<T> C) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= C.total) return;
+    const int b = find_block(C, t);
+    mg_coarsen_point(F.blk[b], C.blk[b], b, t, C,
+                     [&](int, long long f, int, int, int, T& w1, T& w2, T& w3, T& d) {
+                         w1 = F.w1[f]; w2 = F.w2[f]; w3 = F.w3[f]; d = F.dg[f];
+                         return F.dinv[f] != T(0);
+                     },
+                     [&](int, long long f, int, int, int) { return F.dinv[f] != T(0); });
+}
+
+// level 1 straight from the node coefficients (level 0 keeps no arrays of its own)
+template <typename T>
+__global__ void mg_coarsen_fine(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, MGLevelDev<T> F, MGLevelDev<T> C) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= C.total) return;
+    const int b = find_block(C, t);
+    mg_coarsen_point(F.blk[b], C.blk[b], b, t, C,
+                     [&](int bb, long long, int i, int j, int k, T& w1, T& w2, T& w3, T& d) {
+                         return mg_fine_point(g, c, P, vshift, bb, i + 1, j + 1, k + 1, w1, w2, w3, d);
+                     },
+                     [&](int bb, long long, int i, int j, int k) { return mg_fine_active(g, bb, i + 1, j + 1, k + 1); });
 }
 
 // a crossing link is only kept if both aggregates are active
@@ -252,6 +297,209 @@ __global__ void mg_dense(MGLevelDev<T> L, const double* __restrict__ minv, const
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Level-0 kernels on node tiles.  Level 0 of every block is the global unknown
+// vector itself, and its 7-point operators are the self couplings of the rows
+// of qms_operator.cu, so they read the same staged node coefficients instead
+// of stored per-point links:
+//   KIND 0: x = omega D^-1 b                      (first sweep, zero guess)
+//   KIND 1: x_out = x_in + omega D^-1 (b - A x_in)
+//   KIND 2: b_c = sum over each 2x2x2 aggregate of (b - A x_in)  (restriction
+//           fused with the residual; pairs in i via lane shuffles, in j via
+//           shared memory, in k in registers -- no atomics, fixed order)
+// b is scaled pointwise by the row scaling of the outer system when bscale is
+// given; that scaling is the operator diagonal, formed here from the coefficients.
+// x_in is staged in shared memory by cp.async two planes ahead (four
+// components, +-1 halo in i and j); b is fetched into registers one plane ahead.
+// The kernels are instruction-bound at this arithmetic intensity, so the
+// Dirichlet tests are split into a per-thread (i, j) part and a per-plane k
+// part, row indices advance by one add per plane, and D^-1 is a fast
+// reciprocal in FP32 (a preconditioner needs no correctly rounded divide).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T mg_rcp(T d) {
+    if constexpr (sizeof(T) == 4) return __fdividef(1.0f, d);
+    else return T(1) / d;
+}
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? 4 : 2)
+mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __restrict__ b,
+          const float* __restrict__ bscale, const T* __restrict__ xin, T* __restrict__ xout, MGLevelDev<T> C,
+          T* __restrict__ bc) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileCoef<T>& tc = *reinterpret_cast<TileCoef<T>*>(smem_raw);
+    XTile<T>& xt = *reinterpret_cast<XTile<T>*>(smem_raw + sizeof(TileCoef<T>));
+    __shared__ T red[KIND == 2 ? 4 : 1][OTY][OTX];
+    constexpr bool STAGE = KIND != 0;
+    const int i0 = blockIdx.x * OTX + 1, j0 = blockIdx.y * OTY + 1, k0 = blockIdx.z * OKB + 1;
+    const int li = threadIdx.x + 1, lj = threadIdx.y + 1;
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    const bool inij = i <= g.Nx && j <= g.Ny;
+    // per-thread parts of the component predicates (qFixX/Y/Z/V without their k terms)
+    const bool exX = inij && i <= g.xs, exY = inij && j <= g.ys;
+    const bool fxA = i <= 2 || i >= g.Nx - 1, fyA = j <= 2 || j >= g.Ny - 1;
+    const bool fijX = fyA || i == 1 || i == g.xs;
+    const bool fijY = fxA || j == 1 || j == g.ys;
+    const bool fijZ = fxA || fyA;
+    const bool fijV = fxA || fyA || mask_v;
+    const int sXk = g.xs * g.Ny, sYk = g.Nx * g.ys, sZk = g.Nx * g.Ny;
+    // row of each component at plane k0 (32-bit: n_dims < 2^31 is checked at creation)
+    int rX = (i - 1) + (j - 1) * g.xs + (k0 - 1) * sXk;
+    int rY = (int)g.oY + (i - 1) + (j - 1) * g.Nx + (k0 - 1) * sYk;
+    int rZ = (int)g.oZ + (i - 1) + (j - 1) * g.Nx + (k0 - 1) * sZk;
+    int rV = (int)g.oV + (i - 1) + (j - 1) * g.Nx + (k0 - 1) * sZk;
+    const T iscV = bscale ? T(1) / (T(1) + vshift) : T(1);
+    T acc[4] = {T(0), T(0), T(0), T(0)};
+    const int kend = min(k0 + OKB - 1, g.Nz);
+    XStager xsg;
+    CStager csg;
+    if (STAGE) xsg.init(g, i0, j0);
+    csg.init(g, i0, j0);
+    if (STAGE) {
+        xsg.load(g, xin, xt, k0 - 1);
+        xsg.load(g, xin, xt, k0);
+        xsg.load(g, xin, xt, k0 + 1);
+    }
+    csg.load(c, tc, k0 - 1);
+    csg.load(c, tc, k0);
+    T bn0 = T(0), bn1 = T(0), bn2 = T(0), bn3 = T(0);
+    auto fetch_b = [&](int kk, int dX, int dY, int dZ) {
+        bn0 = exX ? __ldg(b + rX + dX) : T(0);
+        bn1 = exY ? __ldg(b + rY + dY) : T(0);
+        bn2 = inij && kk <= g.zs ? __ldg(b + rZ + dZ) : T(0);
+        bn3 = inij && !mask_v ? __ldg(b + rV + dZ) : T(0);
+    };
+    fetch_b(k0, 0, 0, 0);
+    for (int k = k0; k <= kend; k++) {
+        const T b0 = bn0, b1 = bn1, b2 = bn2, b3 = bn3;
+        if (k < kend) fetch_b(k + 1, sXk, sYk, sZk);
+        cp_async_wait_all();
+        __syncthreads();                       // x planes k-1..k+1 and coefficient planes k-1..k ready
+        if (STAGE && k + 2 <= kend + 1) xsg.load(g, xin, xt, k + 2);
+        if (k < kend) csg.load(c, tc, k + 1);
+        const int cur = tslot(k), prv = tslot(k - 1);
+        const int xm = xslot(k - 1), x0 = xslot(k), xp = xslot(k + 1);
+        const bool kfA = k <= 2 || k >= g.Nz - 1;       // k terms of qFixX / qFixY / qFixV
+        const bool kfZ = k == 1 || k == g.zs;           // k term of qFixZ
+#define CF(q, s, dj, di) tc.c[s][q][lj + (dj)][li + (di)]
+#define XS(q, sl, dj, di) xt.v[sl][q][lj + (dj)][li + (di)]
+        T r[4] = {T(0), T(0), T(0), T(0)};
+        // one component: links (wxp, wxm, wyp, wym, wzp, wzm), extra diagonal
+        auto point = [&](int q, bool exists, bool fixed, int row, T bq, T wxp, T wxm, T wyp, T wym, T wzp, T wzm,
+                         T dextra, T dscale, T isc) {
+            if (!exists) return;
+            if (fixed) {
+                if (KIND != 2) xout[row] = T(0);
+                return;
+            }
+            const T d = (wxp + wxm + wyp + wym + wzp + wzm + dextra) * dscale;
+            const T bv = bscale ? bq * d * isc : bq;
+            if (KIND == 0) {
+                xout[row] = omega * bv * mg_rcp(d);
+                return;
+            }
+            const T xc = XS(q, x0, 0, 0);
+            const T Ax = d * xc - wxp * XS(q, x0, 0, 1) - wxm * XS(q, x0, 0, -1) - wyp * XS(q, x0, 1, 0) -
+                         wym * XS(q, x0, -1, 0) - wzp * XS(q, xp, 0, 0) - wzm * XS(q, xm, 0, 0);
+            if (KIND == 2) r[q] = bv - Ax;
+            else xout[row] = xc + omega * (bv - Ax) * mg_rcp(d);
+        };
+        point(0, exX, fijX || kfA, rX, b0,
+              CF(0, cur, 0, 0) * P.idx2, CF(0, cur, 0, -1) * P.idx2, CF(2, cur, 0, 0) * P.idy2,
+              CF(2, cur, -1, 0) * P.idy2, CF(1, cur, 0, 0) * P.idz2, CF(1, prv, 0, 0) * P.idz2,
+              CF(3, cur, 0, 0) * P.idt, T(1), T(1));
+        point(1, exY, fijY || kfA, rY, b1,
+              CF(2, cur, 0, 0) * P.idx2, CF(2, cur, 0, -1) * P.idx2, CF(1, cur, 0, 0) * P.idy2,
+              CF(1, cur, -1, 0) * P.idy2, CF(0, cur, 0, 0) * P.idz2, CF(0, prv, 0, 0) * P.idz2,
+              CF(4, cur, 0, 0) * P.idt, T(1), T(1));
+        point(2, inij && k <= g.zs, fijZ || kfZ, rZ, b2,
+              CF(1, cur, 0, 0) * P.idx2, CF(1, cur, 0, -1) * P.idx2, CF(0, cur, 0, 0) * P.idy2,
+              CF(0, cur, -1, 0) * P.idy2, CF(2, cur, 0, 0) * P.idz2, CF(2, prv, 0, 0) * P.idz2,
+              CF(5, cur, 0, 0) * P.idt, T(1), T(1));
+        {
+            const T fl = P.sigfloor;
+            point(3, inij, fijV || kfA, rV, b3,
+                  fmax(CF(3, cur, 0, 0), fl) * P.idx2, fmax(CF(3, cur, 0, -1), fl) * P.idx2,
+                  fmax(CF(4, cur, 0, 0), fl) * P.idy2, fmax(CF(4, cur, -1, 0), fl) * P.idy2,
+                  fmax(CF(5, cur, 0, 0), fl) * P.idz2, fmax(CF(5, prv, 0, 0), fl) * P.idz2, T(0), T(1) + vshift,
+                  iscV);
+        }
+#undef CF
+#undef XS
+        rX += sXk; rY += sYk; rZ += sZk; rV += sZk;
+        if (KIND == 2) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                r[q] += __shfl_xor_sync(0xffffffffu, r[q], 1);            // i pairs (2p+1, 2p+2)
+                red[q][threadIdx.y][threadIdx.x] = r[q];
+            }
+            __syncthreads();
+            if (!(threadIdx.x & 1) && !(threadIdx.y & 1)) {
+                const bool first = ((k - k0) & 1) == 0;                    // k pairs (odd, even)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const T v = red[q][threadIdx.y][threadIdx.x] + red[q][threadIdx.y + 1][threadIdx.x];
+                    acc[q] = first ? v : acc[q] + v;
+                }
+                if (!first || k == kend) {
+                    const int I = (i - 1) >> 1, J = (j - 1) >> 1, K = (k - 1) >> 1;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const MGBlockDesc& cb = C.blk[q];
+                        if (I < cb.n1 && J < cb.n2 && K < cb.n3)
+                            bc[cb.off + I + (long long)J * cb.n1 + (long long)K * cb.n1 * cb.n2] =
+                                (mask_v && q == 3) ? T(0) : acc[q];
+                    }
+                }
+            }
+        }
+    }
+}
+
+// level 0: x += alpha P x_c on the active points (the Dirichlet points of every component,
+// and V when masked, stay zero); one thread per unknown
+template <typename T>
+__global__ void mg0_prolong(QGrid g, int mask_v, T* __restrict__ x, MGLevelDev<T> C, const T* __restrict__ xc,
+                            T alpha) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n) return;
+    int q, n1, n2;
+    long long o;
+    if (t < g.oY) { q = 0; o = t; n1 = g.xs; n2 = g.Ny; }
+    else if (t < g.oZ) { q = 1; o = t - g.oY; n1 = g.Nx; n2 = g.ys; }
+    else if (t < g.oV) { q = 2; o = t - g.oZ; n1 = g.Nx; n2 = g.Ny; }
+    else { q = 3; o = t - g.oV; n1 = g.Nx; n2 = g.Ny; }
+    const int oi = (int)o;
+    const int i = oi % n1 + 1, j = (oi / n1) % n2 + 1, k = oi / (n1 * n2) + 1;
+    const bool fixed = q == 0 ? qFixX(g, i, j, k) : q == 1 ? qFixY(g, i, j, k) : q == 2 ? qFixZ(g, i, j, k)
+                                                                                   : (mask_v || qFixV(g, i, j, k));
+    if (fixed) return;                    // the sweeps keep these at zero
+    const MGBlockDesc& cb = C.blk[q];
+    x[t] += alpha * xc[cb.off + ((i - 1) >> 1) + (long long)((j - 1) >> 1) * cb.n1 +
+                       (long long)((k - 1) >> 1) * cb.n1 * cb.n2];
+}
+
+template <typename T, int KIND>
+static size_t mg0_smem() {
+    return sizeof(TileCoef<T>) + (KIND != 0 ? sizeof(XTile<T>) : 0);
+}
+
+// raise the dynamic shared-memory limit of the level-0 kernels once per device
+template <typename T>
+static void mg0_prepare() {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    cudaFuncSetAttribute(mg0_tiled<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, 0>());
+    cudaFuncSetAttribute(mg0_tiled<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, 1>());
+    cudaFuncSetAttribute(mg0_tiled<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, 2>());
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -326,8 +574,9 @@ void QmsMG<T>::release() {
 }
 
 template <typename T>
-size_t QmsMG<T>::bytes_for(const QGrid& g, int min_coarse) {
-    // every level stores 8 floats per point (level 0 shares x/b with the Krylov vectors but keeps a temp)
+size_t QmsMG<T>::bytes_for(const QGrid& g, int min_coarse, bool tiled) {
+    // every level stores 8 values per point; a tiled level 0 (stored node coefficients,
+    // more than one level) stores none: its x/b are the Krylov vectors and the caller's temporary
     long long dims[4][3] = {{g.xs, g.Ny, g.Nz}, {g.Nx, g.ys, g.Nz}, {g.Nx, g.Ny, g.zs}, {g.Nx, g.Ny, g.Nz}};
     size_t total = 0;
     for (int l = 0; l < 16; l++) {
@@ -336,11 +585,12 @@ size_t QmsMG<T>::bytes_for(const QGrid& g, int min_coarse) {
             pts += dims[b][0] * dims[b][1] * dims[b][2];
             mx = std::max({mx, dims[b][0], dims[b][1], dims[b][2]});
         }
-        total += (size_t)pts * 8 * sizeof(T);
         if (mx <= min_coarse) {
+            total += (size_t)pts * 8 * sizeof(T);
             total += (size_t)4 * pts * pts * 8 / 4 + 1024;
             break;
         }
+        if (!(tiled && l == 0)) total += (size_t)pts * 8 * sizeof(T);
         for (int b = 0; b < 4; b++) for (int a = 0; a < 3; a++) dims[b][a] = (dims[b][a] + 1) / 2;
     }
     return total;
@@ -367,15 +617,26 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
         if (mx <= min_coarse || (int)lv.size() >= max_levels) break;
         for (int b = 0; b < 4; b++) for (int a = 0; a < 3; a++) dims[b][a] = (dims[b][a] + 1) / 2;
     }
-    for (size_t l = 0; l < lv.size(); l++) {
+    // With stored node coefficients level 0 runs on node tiles (mg0_tiled) and level 1 is
+    // coarsened straight from the coefficients: level 0 keeps no arrays.
+    tiled0 = lv.size() > 1 && c.nc != nullptr;
+    for (size_t l = tiled0 ? 1 : 0; l < lv.size(); l++) {
         MGLevelDev<T>& L = lv[l];
         const size_t bytes = L.total * sizeof(T);
         CKM(cudaMalloc(&L.w1, bytes)); CKM(cudaMalloc(&L.w2, bytes)); CKM(cudaMalloc(&L.w3, bytes));
         CKM(cudaMalloc(&L.dg, bytes)); CKM(cudaMalloc(&L.dinv, bytes)); CKM(cudaMalloc(&L.t, bytes));
         if (l > 0) { CKM(cudaMalloc(&L.x, bytes)); CKM(cudaMalloc(&L.b, bytes)); }
     }
-    mg_fine_coef<<<nblk(lv[0].total), 256, 0, st>>>(g, c, P, vshift, lv[0]);
-    for (size_t l = 1; l < lv.size(); l++) {
+    g0 = g; c0 = c; P0 = P; vshift0 = vshift;
+    g0block = dim3(OTX, OTY, 1);
+    g0grid = dim3((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
+    if (tiled0) {
+        mg_coarsen_fine<<<nblk(lv[1].total), 256, 0, st>>>(g, c, P, vshift, lv[0], lv[1]);
+        mg_mask_links<<<nblk(lv[1].total), 256, 0, st>>>(lv[1]);
+    } else {
+        mg_fine_coef<<<nblk(lv[0].total), 256, 0, st>>>(g, c, P, vshift, lv[0]);
+    }
+    for (size_t l = tiled0 ? 2 : 1; l < lv.size(); l++) {
         mg_coarsen<<<nblk(lv[l].total), 256, 0, st>>>(lv[l - 1], lv[l]);
         mg_mask_links<<<nblk(lv[l].total), 256, 0, st>>>(lv[l]);
     }
@@ -483,6 +744,11 @@ int QmsMG<T>::vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v
     int launches = 0;
     const int nl = (int)lv.size();
     const int mv = mask_v ? 1 : 0;
+    const T* noT = nullptr;
+    if (tiled0) mg0_prepare<T>();
+#define MG0(KIND, B, BS, XI, XO, BC)                                                                          \
+    mg0_tiled<T, KIND><<<g0grid, g0block, mg0_smem<T, KIND>(), st>>>(g0, c0, P0, vshift0, omega, mv, B, BS, XI, \
+                                                                       XO, lv[1], BC)
     for (int l = 0; l < nl; l++) {
         MGLevelDev<T>& L = lv[l];
         const T* b = l == 0 ? b0 : L.b;
@@ -494,17 +760,24 @@ int QmsMG<T>::vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v
             launches++;
             break;
         }
+        // On tiled level 0 the prolongation is in place, so level 0 writes nu1 + nu2
+        // times, alternating buffers: start in t0 when that count is even so that the
+        // last write lands in x0.
+        if (l == 0 && tiled0 && ((nu1 + nu2) % 2 == 0)) std::swap(x, t);
         // pre-smoothing: nu1 Jacobi sweeps from zero; keep the result in x
-        mg_smooth0<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, mv);
+        if (l == 0 && tiled0) MG0(0, b, bs, noT, x, nullptr);
+        else mg_smooth0<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, mv);
         launches++;
         for (int s = 1; s < nu1; s++) {
-            mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, t, mv);
+            if (l == 0 && tiled0) MG0(1, b, bs, x, t, nullptr);
+            else mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, t, mv);
             std::swap(x, t);
             launches++;
         }
         if (l == 0) { cur_x0 = x; cur_t0 = t; }
         else { L.x = x; L.t = t; }
-        mg_restrict<<<nblk(lv[l + 1].total), 256, 0, st>>>(L, b, bs, x, lv[l + 1], lv[l + 1].b, mv);
+        if (l == 0 && tiled0) MG0(2, b, bs, x, nullptr, lv[1].b);
+        else mg_restrict<<<nblk(lv[l + 1].total), 256, 0, st>>>(L, b, bs, x, lv[l + 1], lv[l + 1].b, mv);
         launches++;
     }
     for (int l = nl - 2; l >= 0; l--) {
@@ -513,23 +786,30 @@ int QmsMG<T>::vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v
         const float* bs = l == 0 ? bscale : nullptr;
         T* x = l == 0 ? cur_x0 : L.x;
         T* t = l == 0 ? cur_t0 : L.t;
-        // on level 0 the result must land in x0: the nu2 sweeps alternate buffers, so
-        // prolongate out of place when the parity would end in the temporary
-        const bool flip = l == 0 && (((nu2 % 2 == 0) ? x : t) != x0);
-        if (flip) {
-            mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, x, t, lv[l + 1], lv[l + 1].x, alpha);
-            std::swap(x, t);
+        if (l == 0 && tiled0) {
+            // in place: level 0 then writes nu1 + nu2 times, alternating from the buffer chosen above
+            mg0_prolong<T><<<nblk(g0.n), 256, 0, st>>>(g0, mv, x, lv[1], lv[1].x, alpha);
         } else {
-            mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, x, x, lv[l + 1], lv[l + 1].x, alpha);
+            // untiled: prolongate in place, or out of place when the parity of the nu2
+            // sweeps would leave the level-0 result in the temporary
+            const bool flip = l == 0 && (((nu2 % 2 == 0) ? x : t) != x0);
+            if (flip) {
+                mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, x, t, lv[l + 1], lv[l + 1].x, alpha);
+                std::swap(x, t);
+            } else {
+                mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, x, x, lv[l + 1], lv[l + 1].x, alpha);
+            }
         }
         launches++;
         for (int s = 0; s < nu2; s++) {
-            mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, t, mv);
+            if (l == 0 && tiled0) MG0(1, b, bs, x, t, nullptr);
+            else mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, t, mv);
             std::swap(x, t);
             launches++;
         }
         if (l > 0) { L.x = x; L.t = t; }
     }
+#undef MG0
     return launches;
 }
 

@@ -41,11 +41,18 @@ struct QmsMG {
     int max_levels = 12;
     T* cur_x0 = nullptr;
     T* cur_t0 = nullptr;
+    // level 0 on node tiles (the operator's staged coefficients) instead of stored links
+    bool tiled0 = false;
+    QGrid g0{};
+    QCoef<T> c0{};
+    QStepPar<T> P0{};
+    T vshift0 = T(0);
+    dim3 g0grid, g0block;
     std::string err;
 
     ~QmsMG();
     void release();
-    static size_t bytes_for(const QGrid& g, int min_coarse);
+    static size_t bytes_for(const QGrid& g, int min_coarse, bool tiled);
     int build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T vshift, cudaStream_t st);
     int vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v, cudaStream_t st);
 };

@@ -5,9 +5,12 @@
 // the Ax row (i <= xs), Ay row (j <= ys), Az row (k <= zs) and the V row, with
 // the same entries as the assembled CSR (F:476-607, F:650-781, F:824-955,
 // F:1014-1285 and the transient additions F:1475-1504, F:1624-1681,
-// F:1772-1857, F:1925-2126).  Face 1/mu and edge sigma are formed on the fly
-// from the uint8 material slots (qms_common.cuh), so the only HBM traffic is
-// the input vector, the output vector and one byte per cell.
+// F:1772-1857, F:1925-2126).  Face 1/mu and edge sigma come from the six stored
+// node coefficients (or are formed on the fly from the uint8 material slots when
+// none are stored), so the HBM traffic per node is the four inputs, the four
+// outputs and the six coefficients.  The four unknown components of three
+// k-planes (plus one in flight) sit in shared memory, staged by cp.async, so
+// every neighbour read of the 17/37-point rows is a shared-memory read.
 //
 // Modes:
 //   QOP_APPLY   y = M x                       (Dirichlet rows: y = x)
@@ -17,7 +20,9 @@
 //   APPLY/SCALED: [0] += y . w, [1] += y . y    (w may be null -> skip)
 //   RESID:        [0] += |r_A|^2, [1] += |r_V|^2, [2] += |x_A|^2, [3] += |x_V|^2
 #include "qms_internal.h"
+#include "qms_tile.cuh"
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 enum QOpMode { QOP_APPLY = 0, QOP_SCALED = 1, QOP_RESID = 2 };
@@ -31,59 +36,44 @@ enum QOpMode { QOP_APPLY = 0, QOP_SCALED = 1, QOP_RESID = 2 };
 // ring instead of once per use (each coefficient is used by up to 8 rows).
 // Unknowns are read through L1; index arithmetic is 32-bit within a block.
 // ---------------------------------------------------------------------------
-#define OTX 32
-#define OTY 8
-#define OKB 16
-
+// D^-1 of the scaled FP32 operator: a fast divide (the inner solver only needs the
+// same operator on every application, which any deterministic rounding gives); FP64 exact
 template <typename T>
-struct TileCoef {
-    T c[2][6][OTY + 1][OTX + 1];
-};
-
-template <typename T>
-__device__ __forceinline__ void tile_fill_plane(const QCoef<T>& c, TileCoef<T>& tc, int slot, int i0, int j0, int k) {
-    const int tid = threadIdx.x + OTX * threadIdx.y;
-    for (int q = tid; q < (OTX + 1) * (OTY + 1); q += OTX * OTY) {
-        const int li = q % (OTX + 1), lj = q / (OTX + 1);
-        const int i = i0 - 1 + li, j = j0 - 1 + lj;
-        T v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
-        if (i >= 1 && j >= 1 && k >= 1 && i <= c.g.Nx && j <= c.g.Ny && k <= c.g.Nz) {
-            v0 = c.imux(i, j, k); v1 = c.imuy(i, j, k); v2 = c.imuz(i, j, k);
-            v3 = c.sgx(i, j, k); v4 = c.sgy(i, j, k); v5 = c.sgz(i, j, k);
-        }
-        tc.c[slot][0][lj][li] = v0; tc.c[slot][1][lj][li] = v1; tc.c[slot][2][lj][li] = v2;
-        tc.c[slot][3][lj][li] = v3; tc.c[slot][4][lj][li] = v4; tc.c[slot][5][lj][li] = v5;
-    }
+__device__ __forceinline__ T op_div(T a, T d) {
+    if constexpr (sizeof(T) == 4) return __fdividef(a, d);
+    else return a / d;
 }
 
 template <typename T, bool ADV, int MODE>
-__global__ void __launch_bounds__(OTX * OTY)
+__global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? 4 : 2)
 qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const T* __restrict__ b,
               T* __restrict__ y, const T* __restrict__ w, double* __restrict__ partials) {
-    __shared__ TileCoef<T> tc;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileCoef<T>& tc = *reinterpret_cast<TileCoef<T>*>(smem_raw);
+    XTile<T>& xt = *reinterpret_cast<XTile<T>*>(smem_raw + sizeof(TileCoef<T>));
     const int i0 = blockIdx.x * OTX + 1, j0 = blockIdx.y * OTY + 1, k0 = blockIdx.z * OKB + 1;
     const int li = threadIdx.x + 1, lj = threadIdx.y + 1;   // position in the coefficient tile
     const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
     const bool inij = i <= g.Nx && j <= g.Ny;
-    // block bases and 32-bit strides of the four unknown blocks
-    const T* __restrict__ xX = x;
-    const T* __restrict__ xY = x + g.oY;
-    const T* __restrict__ xZ = x + g.oZ;
-    const T* __restrict__ xV = x + g.oV;
+    // 32-bit strides of the four unknown blocks (row indices of this thread's unknowns)
+    // (i, j) parts of the Dirichlet predicates qFixX/Y/Z/V; their k parts are per plane
+    const bool fxA = i <= 2 || i >= g.Nx - 1, fyA = j <= 2 || j >= g.Ny - 1;
+    const bool fijX = fyA || i == 1 || i == g.xs, fijY = fxA || j == 1 || j == g.ys, fijZ = fxA || fyA;
     const int sXj = g.xs, sXk = g.xs * g.Ny;      // Ax: (xs, Ny, Nz)
     const int sYj = g.Nx, sYk = g.Nx * g.ys;      // Ay: (Nx, ys, Nz)
     const int sZj = g.Nx, sZk = g.Nx * g.Ny;      // Az: (Nx, Ny, zs); V: (Nx, Ny, Nz)
     using RT = typename std::conditional<MODE == QOP_RESID, double, float>::type;
     RT red0 = 0, red1 = 0, red2 = 0, red3 = 0;
-    auto emit = [&](long long row, T acc, T diag, bool is_a) {
+    T xc_center = T(0);
+    auto emit = [&](int row, T acc, T diag, bool is_a) {
         T out;
         if (MODE == QOP_APPLY) out = acc;
-        else if (MODE == QOP_SCALED) out = acc / diag;
+        else if (MODE == QOP_SCALED) out = op_div(acc, diag);
         else out = (b[row] - acc) / diag;
         y[row] = out;
         if (partials) {
             if (MODE == QOP_RESID) {
-                RT o = (RT)out, xv = (RT)__ldg(x + row);
+                RT o = (RT)out, xv = (RT)xc_center;
                 if (is_a) { red0 += o * o; red2 += xv * xv; }
                 else { red1 += o * o; red3 += xv * xv; }
             } else {
@@ -92,20 +82,39 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
             }
         }
     };
-    tile_fill_plane(c, tc, (k0 - 1) & 1, i0, j0, k0 - 1);
+    XStager xsg;
+    CStager csg;
+    xsg.init(g, i0, j0);
+    csg.init(g, i0, j0);
+    xsg.load(g, x, xt, k0 - 1);
+    xsg.load(g, x, xt, k0);
+    xsg.load(g, x, xt, k0 + 1);
+    csg.load(c, tc, k0 - 1);
+    csg.load(c, tc, k0);
     const int kend = min(k0 + OKB - 1, g.Nz);
+    // rows of this thread's four unknowns at plane k0 (32-bit: n_dims < 2^31 is checked at creation)
+    int rX = (i - 1) + (j - 1) * sXj + (k0 - 1) * sXk;
+    int rY = (int)g.oY + (i - 1) + (j - 1) * sYj + (k0 - 1) * sYk;
+    int rZ = (int)g.oZ + (i - 1) + (j - 1) * sZj + (k0 - 1) * sZk;
+    int rV = (int)g.oV + (i - 1) + (j - 1) * sZj + (k0 - 1) * sZk;
     for (int k = k0; k <= kend; k++) {
-        const int cur = k & 1, prv = (k - 1) & 1;
-        tile_fill_plane(c, tc, cur, i0, j0, k);
-        __syncthreads();
+        const bool kfA = k <= 2 || k >= g.Nz - 1;       // k terms of qFixX / qFixY / qFixV
+        const bool kfZ = k == 1 || k == g.zs;           // k term of qFixZ
+        cp_async_wait_all();
+        __syncthreads();                       // planes k-1..k+1 of x and k-1..k of the coefficients ready
+        if (k + 2 <= kend + 1) xsg.load(g, x, xt, k + 2);   // x plane k+2 into the slot of plane k-2
+        if (k < kend) csg.load(c, tc, k + 1);                // coefficients of plane k+1 into that of k-2
+        const int cur = tslot(k), prv = tslot(k - 1);
+        const int xm = xslot(k - 1), x0 = xslot(k), xp = xslot(k + 1);
 #define CF(q, s, dj, di) tc.c[s][q][lj + (dj)][li + (di)]
+#define XS(comp, sl, dj, di) xt.v[sl][comp][lj + (dj)][li + (di)]
         if (inij) {
             // ---------------------------------------------------------------- Ax
             if (i <= g.xs) {
-                const int o = (i - 1) + (j - 1) * sXj + (k - 1) * sXk;
-                const long long row = o;
-                if (qFixX(g, i, j, k)) {
-                    emit(row, __ldg(xX + o), T(1), true);
+                const int row = rX;
+                xc_center = XS(0, x0, 0, 0);
+                if (fijX || kfA) {
+                    emit(row, XS(0, x0, 0, 0), T(1), true);
                 } else {
                     const T s = CF(3, cur, 0, 0);
                     const T my_km = CF(1, prv, 0, 0), my_k = CF(1, cur, 0, 0);
@@ -113,33 +122,31 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T mx_im = CF(0, cur, 0, -1), mx_i = CF(0, cur, 0, 0);
                     const T svy = ADV ? s * P.vy : T(0), svz = ADV ? s * P.vz : T(0);
                     const T d = (mz_j + mz_jm) * P.idy2 + (my_k + my_km) * P.idz2 + (mx_i + mx_im) * P.idx2 + s * P.idt;
-                    const int oy = (i - 1) + (j - 1) * sYj + (k - 1) * sYk;
-                    const int oz = (i - 1) + (j - 1) * sZj + (k - 1) * sZk;
-                    T acc = d * __ldg(xX + o);
-                    acc += (-my_km * P.idz2 + svz * P.i2dz) * __ldg(xX + o - sXk);
-                    acc += (-mz_jm * P.idy2 + svy * P.i2dy) * __ldg(xX + o - sXj);
-                    acc += (-mx_im * P.idx2) * __ldg(xX + o - 1);
-                    acc += (-mx_i * P.idx2) * __ldg(xX + o + 1);
-                    acc += (-mz_j * P.idy2 - svy * P.i2dy) * __ldg(xX + o + sXj);
-                    acc += (-my_k * P.idz2 - svz * P.i2dz) * __ldg(xX + o + sXk);
-                    acc += (mz_jm * P.idxdy - svy * P.i2dx) * __ldg(xY + oy - sYj);
-                    acc += (-mz_jm * P.idxdy + svy * P.i2dx) * __ldg(xY + oy - sYj + 1);
-                    acc += (-mz_j * P.idxdy - svy * P.i2dx) * __ldg(xY + oy);
-                    acc += (mz_j * P.idxdy + svy * P.i2dx) * __ldg(xY + oy + 1);
-                    acc += (my_km * P.idxdz - svz * P.i2dx) * __ldg(xZ + oz - sZk);
-                    acc += (-my_km * P.idxdz + svz * P.i2dx) * __ldg(xZ + oz - sZk + 1);
-                    acc += (-my_k * P.idxdz - svz * P.i2dx) * __ldg(xZ + oz);
-                    acc += (my_k * P.idxdz + svz * P.i2dx) * __ldg(xZ + oz + 1);
-                    acc += s * P.idx * (__ldg(xV + oz + 1) - __ldg(xV + oz));
+                    T acc = d * XS(0, x0, 0, 0);
+                    acc += (-my_km * P.idz2 + svz * P.i2dz) * XS(0, xm, 0, 0);
+                    acc += (-mz_jm * P.idy2 + svy * P.i2dy) * XS(0, x0, -1, 0);
+                    acc += (-mx_im * P.idx2) * XS(0, x0, 0, -1);
+                    acc += (-mx_i * P.idx2) * XS(0, x0, 0, 1);
+                    acc += (-mz_j * P.idy2 - svy * P.i2dy) * XS(0, x0, 1, 0);
+                    acc += (-my_k * P.idz2 - svz * P.i2dz) * XS(0, xp, 0, 0);
+                    acc += (mz_jm * P.idxdy - svy * P.i2dx) * XS(1, x0, -1, 0);
+                    acc += (-mz_jm * P.idxdy + svy * P.i2dx) * XS(1, x0, -1, 1);
+                    acc += (-mz_j * P.idxdy - svy * P.i2dx) * XS(1, x0, 0, 0);
+                    acc += (mz_j * P.idxdy + svy * P.i2dx) * XS(1, x0, 0, 1);
+                    acc += (my_km * P.idxdz - svz * P.i2dx) * XS(2, xm, 0, 0);
+                    acc += (-my_km * P.idxdz + svz * P.i2dx) * XS(2, xm, 0, 1);
+                    acc += (-my_k * P.idxdz - svz * P.i2dx) * XS(2, x0, 0, 0);
+                    acc += (my_k * P.idxdz + svz * P.i2dx) * XS(2, x0, 0, 1);
+                    acc += s * P.idx * (XS(3, x0, 0, 1) - XS(3, x0, 0, 0));
                     emit(row, acc, d, true);
                 }
             }
             // ---------------------------------------------------------------- Ay
             if (j <= g.ys) {
-                const int o = (i - 1) + (j - 1) * sYj + (k - 1) * sYk;
-                const long long row = g.oY + o;
-                if (qFixY(g, i, j, k)) {
-                    emit(row, __ldg(xY + o), T(1), true);
+                const int row = rY;
+                xc_center = XS(1, x0, 0, 0);
+                if (fijY || kfA) {
+                    emit(row, XS(1, x0, 0, 0), T(1), true);
                 } else {
                     const T s = CF(4, cur, 0, 0);
                     const T mz_im = CF(2, cur, 0, -1), mz_i = CF(2, cur, 0, 0);
@@ -147,33 +154,31 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T my_jm = CF(1, cur, -1, 0), my_j = CF(1, cur, 0, 0);
                     const T svx = ADV ? s * P.vx : T(0), svz = ADV ? s * P.vz : T(0);
                     const T d = (mz_i + mz_im) * P.idx2 + (mx_k + mx_km) * P.idz2 + (my_j + my_jm) * P.idy2 + s * P.idt;
-                    const int ox = (i - 1) + (j - 1) * sXj + (k - 1) * sXk;
-                    const int oz = (i - 1) + (j - 1) * sZj + (k - 1) * sZk;
-                    T acc = d * __ldg(xY + o);
-                    acc += (mz_im * P.idxdy - svx * P.i2dy) * __ldg(xX + ox - 1);
-                    acc += (-mz_i * P.idxdy - svx * P.i2dy) * __ldg(xX + ox);
-                    acc += (-mz_im * P.idxdy + svx * P.i2dy) * __ldg(xX + ox + sXj - 1);
-                    acc += (mz_i * P.idxdy + svx * P.i2dy) * __ldg(xX + ox + sXj);
-                    acc += (-mx_km * P.idz2 + svz * P.i2dz) * __ldg(xY + o - sYk);
-                    acc += (-my_jm * P.idy2) * __ldg(xY + o - sYj);
-                    acc += (-mz_im * P.idx2 + svx * P.i2dx) * __ldg(xY + o - 1);
-                    acc += (-mz_i * P.idx2 - svx * P.i2dx) * __ldg(xY + o + 1);
-                    acc += (-my_j * P.idy2) * __ldg(xY + o + sYj);
-                    acc += (-mx_k * P.idz2 - svz * P.i2dz) * __ldg(xY + o + sYk);
-                    acc += (mx_km * P.idydz - svz * P.i2dy) * __ldg(xZ + oz - sZk);
-                    acc += (-mx_km * P.idydz + svz * P.i2dy) * __ldg(xZ + oz - sZk + sZj);
-                    acc += (-mx_k * P.idydz - svz * P.i2dy) * __ldg(xZ + oz);
-                    acc += (mx_k * P.idydz + svz * P.i2dy) * __ldg(xZ + oz + sZj);
-                    acc += s * P.idy * (__ldg(xV + oz + sZj) - __ldg(xV + oz));
+                    T acc = d * XS(1, x0, 0, 0);
+                    acc += (mz_im * P.idxdy - svx * P.i2dy) * XS(0, x0, 0, -1);
+                    acc += (-mz_i * P.idxdy - svx * P.i2dy) * XS(0, x0, 0, 0);
+                    acc += (-mz_im * P.idxdy + svx * P.i2dy) * XS(0, x0, 1, -1);
+                    acc += (mz_i * P.idxdy + svx * P.i2dy) * XS(0, x0, 1, 0);
+                    acc += (-mx_km * P.idz2 + svz * P.i2dz) * XS(1, xm, 0, 0);
+                    acc += (-my_jm * P.idy2) * XS(1, x0, -1, 0);
+                    acc += (-mz_im * P.idx2 + svx * P.i2dx) * XS(1, x0, 0, -1);
+                    acc += (-mz_i * P.idx2 - svx * P.i2dx) * XS(1, x0, 0, 1);
+                    acc += (-my_j * P.idy2) * XS(1, x0, 1, 0);
+                    acc += (-mx_k * P.idz2 - svz * P.i2dz) * XS(1, xp, 0, 0);
+                    acc += (mx_km * P.idydz - svz * P.i2dy) * XS(2, xm, 0, 0);
+                    acc += (-mx_km * P.idydz + svz * P.i2dy) * XS(2, xm, 1, 0);
+                    acc += (-mx_k * P.idydz - svz * P.i2dy) * XS(2, x0, 0, 0);
+                    acc += (mx_k * P.idydz + svz * P.i2dy) * XS(2, x0, 1, 0);
+                    acc += s * P.idy * (XS(3, x0, 1, 0) - XS(3, x0, 0, 0));
                     emit(row, acc, d, true);
                 }
             }
             // ---------------------------------------------------------------- Az
             if (k <= g.zs) {
-                const int o = (i - 1) + (j - 1) * sZj + (k - 1) * sZk;
-                const long long row = g.oZ + o;
-                if (qFixZ(g, i, j, k)) {
-                    emit(row, __ldg(xZ + o), T(1), true);
+                const int row = rZ;
+                xc_center = XS(2, x0, 0, 0);
+                if (fijZ || kfZ) {
+                    emit(row, XS(2, x0, 0, 0), T(1), true);
                 } else {
                     const T s = CF(5, cur, 0, 0);
                     const T my_im = CF(1, cur, 0, -1), my_i = CF(1, cur, 0, 0);
@@ -181,33 +186,31 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T mz_km = CF(2, prv, 0, 0), mz_k = CF(2, cur, 0, 0);
                     const T svx = ADV ? s * P.vx : T(0), svy = ADV ? s * P.vy : T(0);
                     const T d = (my_i + my_im) * P.idx2 + (mx_j + mx_jm) * P.idy2 + (mz_k + mz_km) * P.idz2 + s * P.idt;
-                    const int ox = (i - 1) + (j - 1) * sXj + (k - 1) * sXk;
-                    const int oy = (i - 1) + (j - 1) * sYj + (k - 1) * sYk;
-                    T acc = d * __ldg(xZ + o);
-                    acc += (my_im * P.idxdz - svx * P.i2dz) * __ldg(xX + ox - 1);
-                    acc += (-my_i * P.idxdz - svx * P.i2dz) * __ldg(xX + ox);
-                    acc += (-my_im * P.idxdz + svx * P.i2dz) * __ldg(xX + ox + sXk - 1);
-                    acc += (my_i * P.idxdz + svx * P.i2dz) * __ldg(xX + ox + sXk);
-                    acc += (mx_jm * P.idydz - svy * P.i2dz) * __ldg(xY + oy - sYj);
-                    acc += (-mx_j * P.idydz - svy * P.i2dz) * __ldg(xY + oy);
-                    acc += (-mx_jm * P.idydz + svy * P.i2dz) * __ldg(xY + oy - sYj + sYk);
-                    acc += (mx_j * P.idydz + svy * P.i2dz) * __ldg(xY + oy + sYk);
-                    acc += (-mz_km * P.idz2) * __ldg(xZ + o - sZk);
-                    acc += (-mx_jm * P.idy2 + svy * P.i2dy) * __ldg(xZ + o - sZj);
-                    acc += (-my_im * P.idx2 + svx * P.i2dx) * __ldg(xZ + o - 1);
-                    acc += (-my_i * P.idx2 - svx * P.i2dx) * __ldg(xZ + o + 1);
-                    acc += (-mx_j * P.idy2 - svy * P.i2dy) * __ldg(xZ + o + sZj);
-                    acc += (-mz_k * P.idz2) * __ldg(xZ + o + sZk);
-                    acc += s * P.idz * (__ldg(xV + o + sZk) - __ldg(xV + o));
+                    T acc = d * XS(2, x0, 0, 0);
+                    acc += (my_im * P.idxdz - svx * P.i2dz) * XS(0, x0, 0, -1);
+                    acc += (-my_i * P.idxdz - svx * P.i2dz) * XS(0, x0, 0, 0);
+                    acc += (-my_im * P.idxdz + svx * P.i2dz) * XS(0, xp, 0, -1);
+                    acc += (my_i * P.idxdz + svx * P.i2dz) * XS(0, xp, 0, 0);
+                    acc += (mx_jm * P.idydz - svy * P.i2dz) * XS(1, x0, -1, 0);
+                    acc += (-mx_j * P.idydz - svy * P.i2dz) * XS(1, x0, 0, 0);
+                    acc += (-mx_jm * P.idydz + svy * P.i2dz) * XS(1, xp, -1, 0);
+                    acc += (mx_j * P.idydz + svy * P.i2dz) * XS(1, xp, 0, 0);
+                    acc += (-mz_km * P.idz2) * XS(2, xm, 0, 0);
+                    acc += (-mx_jm * P.idy2 + svy * P.i2dy) * XS(2, x0, -1, 0);
+                    acc += (-my_im * P.idx2 + svx * P.i2dx) * XS(2, x0, 0, -1);
+                    acc += (-my_i * P.idx2 - svx * P.i2dx) * XS(2, x0, 0, 1);
+                    acc += (-mx_j * P.idy2 - svy * P.i2dy) * XS(2, x0, 1, 0);
+                    acc += (-mz_k * P.idz2) * XS(2, xp, 0, 0);
+                    acc += s * P.idz * (XS(3, xp, 0, 0) - XS(3, x0, 0, 0));
                     emit(row, acc, d, true);
                 }
             }
             // ---------------------------------------------------------------- V
             {
-                const int o = (i - 1) + (j - 1) * sZj + (k - 1) * sZk;
-                const long long row = g.oV + o;
-                if (qFixV(g, i, j, k)) {
-                    emit(row, __ldg(xV + o), T(1), false);
+                const int row = rV;
+                xc_center = XS(3, x0, 0, 0);
+                if (fijZ || kfA) {
+                    emit(row, XS(3, x0, 0, 0), T(1), false);
                 } else {
                     const T sx0 = CF(3, cur, 0, 0), sx1 = CF(3, cur, 0, -1);
                     const T sy0 = CF(4, cur, 0, 0), sy1 = CF(4, cur, -1, 0);
@@ -216,58 +219,57 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T fy0 = fmax(sy0, P.sigfloor), fy1 = fmax(sy1, P.sigfloor);
                     const T fz0 = fmax(sz0, P.sigfloor), fz1 = fmax(sz1, P.sigfloor);
                     const T d = (fx0 + fx1) * P.idx2 + (fy0 + fy1) * P.idy2 + (fz0 + fz1) * P.idz2;
-                    const int ox = (i - 1) + (j - 1) * sXj + (k - 1) * sXk;
-                    const int oy = (i - 1) + (j - 1) * sYj + (k - 1) * sYk;
-                    T acc = d * __ldg(xV + o);
-                    acc -= fz1 * P.idz2 * __ldg(xV + o - sZk);
-                    acc -= fy1 * P.idy2 * __ldg(xV + o - sZj);
-                    acc -= fx1 * P.idx2 * __ldg(xV + o - 1);
-                    acc -= fx0 * P.idx2 * __ldg(xV + o + 1);
-                    acc -= fy0 * P.idy2 * __ldg(xV + o + sZj);
-                    acc -= fz0 * P.idz2 * __ldg(xV + o + sZk);
-                    const T axm = __ldg(xX + ox - 1), ax0 = __ldg(xX + ox);
-                    const T aym = __ldg(xY + oy - sYj), ay0 = __ldg(xY + oy);
-                    const T azm = __ldg(xZ + o - sZk), az0 = __ldg(xZ + o);
+                    T acc = d * XS(3, x0, 0, 0);
+                    acc -= fz1 * P.idz2 * XS(3, xm, 0, 0);
+                    acc -= fy1 * P.idy2 * XS(3, x0, -1, 0);
+                    acc -= fx1 * P.idx2 * XS(3, x0, 0, -1);
+                    acc -= fx0 * P.idx2 * XS(3, x0, 0, 1);
+                    acc -= fy0 * P.idy2 * XS(3, x0, 1, 0);
+                    acc -= fz0 * P.idz2 * XS(3, xp, 0, 0);
+                    const T axm = XS(0, x0, 0, -1), ax0 = XS(0, x0, 0, 0);
+                    const T aym = XS(1, x0, -1, 0), ay0 = XS(1, x0, 0, 0);
+                    const T azm = XS(2, xm, 0, 0), az0 = XS(2, x0, 0, 0);
                     acc += P.idt * ((sx0 * ax0 - sx1 * axm) * P.idx + (sy0 * ay0 - sy1 * aym) * P.idy +
                                     (sz0 * az0 - sz1 * azm) * P.idz);
                     if (ADV) {
                         const T vx = P.vx, vy = P.vy, vz = P.vz;
-                        acc += (sx1 * vz * P.i2dxdz - sz1 * vx * P.i2dz2) * __ldg(xX + ox - 1 - sXk);
-                        acc += (-sx0 * vz * P.i2dxdz - sz1 * vx * P.i2dz2) * __ldg(xX + ox - sXk);
-                        acc += (sx1 * vy * P.i2dxdy - sy1 * vx * P.i2dy2) * __ldg(xX + ox - 1 - sXj);
-                        acc += (-sx0 * vy * P.i2dxdy - sy1 * vx * P.i2dy2) * __ldg(xX + ox - sXj);
+                        acc += (sx1 * vz * P.i2dxdz - sz1 * vx * P.i2dz2) * XS(0, xm, 0, -1);
+                        acc += (-sx0 * vz * P.i2dxdz - sz1 * vx * P.i2dz2) * XS(0, xm, 0, 0);
+                        acc += (sx1 * vy * P.i2dxdy - sy1 * vx * P.i2dy2) * XS(0, x0, -1, -1);
+                        acc += (-sx0 * vy * P.i2dxdy - sy1 * vx * P.i2dy2) * XS(0, x0, -1, 0);
                         acc += ((sy0 + sy1) * vx * P.i2dy2 + (sz0 + sz1) * vx * P.i2dz2) * (axm + ax0);
-                        acc += (-sx1 * vy * P.i2dxdy - sy0 * vx * P.i2dy2) * __ldg(xX + ox - 1 + sXj);
-                        acc += (sx0 * vy * P.i2dxdy - sy0 * vx * P.i2dy2) * __ldg(xX + ox + sXj);
-                        acc += (-sx1 * vz * P.i2dxdz - sz0 * vx * P.i2dz2) * __ldg(xX + ox - 1 + sXk);
-                        acc += (sx0 * vz * P.i2dxdz - sz0 * vx * P.i2dz2) * __ldg(xX + ox + sXk);
+                        acc += (-sx1 * vy * P.i2dxdy - sy0 * vx * P.i2dy2) * XS(0, x0, 1, -1);
+                        acc += (sx0 * vy * P.i2dxdy - sy0 * vx * P.i2dy2) * XS(0, x0, 1, 0);
+                        acc += (-sx1 * vz * P.i2dxdz - sz0 * vx * P.i2dz2) * XS(0, xp, 0, -1);
+                        acc += (sx0 * vz * P.i2dxdz - sz0 * vx * P.i2dz2) * XS(0, xp, 0, 0);
 
-                        acc += (sy1 * vz * P.i2dydz - sz1 * vy * P.i2dz2) * __ldg(xY + oy - sYj - sYk);
-                        acc += (-sy0 * vz * P.i2dydz - sz1 * vy * P.i2dz2) * __ldg(xY + oy - sYk);
-                        acc += (-sx1 * vy * P.i2dx2 + sy1 * vx * P.i2dxdy) * __ldg(xY + oy - sYj - 1);
+                        acc += (sy1 * vz * P.i2dydz - sz1 * vy * P.i2dz2) * XS(1, xm, -1, 0);
+                        acc += (-sy0 * vz * P.i2dydz - sz1 * vy * P.i2dz2) * XS(1, xm, 0, 0);
+                        acc += (-sx1 * vy * P.i2dx2 + sy1 * vx * P.i2dxdy) * XS(1, x0, -1, -1);
                         acc += ((sx0 + sx1) * vy * P.i2dx2 + (sz0 + sz1) * vy * P.i2dz2) * (aym + ay0);
-                        acc += (-sx0 * vy * P.i2dx2 - sy1 * vx * P.i2dxdy) * __ldg(xY + oy - sYj + 1);
-                        acc += (-sx1 * vy * P.i2dx2 - sy0 * vx * P.i2dxdy) * __ldg(xY + oy - 1);
-                        acc += (-sx0 * vy * P.i2dx2 + sy0 * vx * P.i2dxdy) * __ldg(xY + oy + 1);
-                        acc += (-sy1 * vz * P.i2dydz - sz0 * vy * P.i2dz2) * __ldg(xY + oy - sYj + sYk);
-                        acc += (sy0 * vz * P.i2dydz - sz0 * vy * P.i2dz2) * __ldg(xY + oy + sYk);
+                        acc += (-sx0 * vy * P.i2dx2 - sy1 * vx * P.i2dxdy) * XS(1, x0, -1, 1);
+                        acc += (-sx1 * vy * P.i2dx2 - sy0 * vx * P.i2dxdy) * XS(1, x0, 0, -1);
+                        acc += (-sx0 * vy * P.i2dx2 + sy0 * vx * P.i2dxdy) * XS(1, x0, 0, 1);
+                        acc += (-sy1 * vz * P.i2dydz - sz0 * vy * P.i2dz2) * XS(1, xp, -1, 0);
+                        acc += (sy0 * vz * P.i2dydz - sz0 * vy * P.i2dz2) * XS(1, xp, 0, 0);
 
-                        acc += (-sy1 * vz * P.i2dy2 + sz1 * vy * P.i2dydz) * __ldg(xZ + o - sZj - sZk);
-                        acc += (-sx1 * vz * P.i2dx2 + sz1 * vx * P.i2dxdz) * __ldg(xZ + o - 1 - sZk);
+                        acc += (-sy1 * vz * P.i2dy2 + sz1 * vy * P.i2dydz) * XS(2, xm, -1, 0);
+                        acc += (-sx1 * vz * P.i2dx2 + sz1 * vx * P.i2dxdz) * XS(2, xm, 0, -1);
                         acc += ((sx0 + sx1) * vz * P.i2dx2 + (sy0 + sy1) * vz * P.i2dy2) * (azm + az0);
-                        acc += (-sx0 * vz * P.i2dx2 - sz1 * vx * P.i2dxdz) * __ldg(xZ + o + 1 - sZk);
-                        acc += (-sy0 * vz * P.i2dy2 - sz1 * vy * P.i2dydz) * __ldg(xZ + o + sZj - sZk);
-                        acc += (-sy1 * vz * P.i2dy2 - sz0 * vy * P.i2dydz) * __ldg(xZ + o - sZj);
-                        acc += (-sx1 * vz * P.i2dx2 - sz0 * vx * P.i2dxdz) * __ldg(xZ + o - 1);
-                        acc += (-sx0 * vz * P.i2dx2 + sz0 * vx * P.i2dxdz) * __ldg(xZ + o + 1);
-                        acc += (-sy0 * vz * P.i2dy2 + sz0 * vy * P.i2dydz) * __ldg(xZ + o + sZj);
+                        acc += (-sx0 * vz * P.i2dx2 - sz1 * vx * P.i2dxdz) * XS(2, xm, 0, 1);
+                        acc += (-sy0 * vz * P.i2dy2 - sz1 * vy * P.i2dydz) * XS(2, xm, 1, 0);
+                        acc += (-sy1 * vz * P.i2dy2 - sz0 * vy * P.i2dydz) * XS(2, x0, -1, 0);
+                        acc += (-sx1 * vz * P.i2dx2 - sz0 * vx * P.i2dxdz) * XS(2, x0, 0, -1);
+                        acc += (-sx0 * vz * P.i2dx2 + sz0 * vx * P.i2dxdz) * XS(2, x0, 0, 1);
+                        acc += (-sy0 * vz * P.i2dy2 + sz0 * vy * P.i2dydz) * XS(2, x0, 1, 0);
                     }
                     emit(row, acc, d, false);
                 }
             }
         }
 #undef CF
-        __syncthreads();
+#undef XS
+        rX += sXk; rY += sYk; rZ += sZk; rV += sZk;
     }
     if (partials) {
         __shared__ double sh[32];
@@ -284,6 +286,20 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
             if (qLinTid() == 0) partials[3 * nb + bid] = s3;
         }
     }
+}
+
+// The six node coefficients, formed once per geometry from the material slots.
+template <typename T>
+__global__ void qk_node_coef(QGrid g, QCoef<T> c, T* __restrict__ nc) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.Nn) return;
+    const int i = (int)(t % g.Nx) + 1, j = (int)((t / g.Nx) % g.Ny) + 1, k = (int)(t / ((long long)g.Nx * g.Ny)) + 1;
+    nc[t] = c.imux(i, j, k);
+    nc[g.Nn + t] = c.imuy(i, j, k);
+    nc[2 * g.Nn + t] = c.imuz(i, j, k);
+    nc[3 * g.Nn + t] = c.sgx(i, j, k);
+    nc[4 * g.Nn + t] = c.sgy(i, j, k);
+    nc[5 * g.Nn + t] = c.sgz(i, j, k);
 }
 
 // Diagonal of the (steady or transient) operator, FP32, for the Jacobi
@@ -350,11 +366,32 @@ long long qms_op_num_blocks(const QGrid& g) {
     return (long long)t.x * t.y * t.z;
 }
 
+// The operator's tiles exceed the 48 KB default of dynamic shared memory in FP64: raise the
+// limit of all six instances once per device (before any stream capture of a launch).
+template <typename T>
+static void qms_operator_prepare() {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    const int shm = (int)(sizeof(TileCoef<T>) + sizeof(XTile<T>));
+    cudaFuncSetAttribute(qk_operator_t<T, false, QOP_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_operator_t<T, false, QOP_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_operator_t<T, false, QOP_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_operator_t<T, true, QOP_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_operator_t<T, true, QOP_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_operator_t<T, true, QOP_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
 template <typename T>
 void qms_launch_operator(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, bool adv, int mode, const T* x,
                          const T* b, T* y, const T* w, double* partials, cudaStream_t st) {
     dim3 bs = opt_block(), gs = opt_grid(g);
-#define L(ADV, MODE) qk_operator_t<T, ADV, MODE><<<gs, bs, 0, st>>>(g, c, P, x, b, y, w, partials)
+    const size_t shm = sizeof(TileCoef<T>) + sizeof(XTile<T>);
+    qms_operator_prepare<T>();
+#define L(ADV, MODE) qk_operator_t<T, ADV, MODE><<<gs, bs, shm, st>>>(g, c, P, x, b, y, w, partials)
     if (adv) {
         if (mode == QOP_APPLY) L(true, QOP_APPLY);
         else if (mode == QOP_SCALED) L(true, QOP_SCALED);
@@ -371,6 +408,15 @@ template void qms_launch_operator<float>(const QGrid&, const QCoef<float>&, cons
                                          const float*, const float*, float*, const float*, double*, cudaStream_t);
 template void qms_launch_operator<double>(const QGrid&, const QCoef<double>&, const QStepPar<double>&, bool, int,
                                           const double*, const double*, double*, const double*, double*, cudaStream_t);
+
+template <typename T>
+void qms_launch_node_coef(const QGrid& g, const QCoef<T>& c, T* nc, cudaStream_t st) {
+    QCoef<T> c0 = c;
+    c0.nc = nullptr;
+    qk_node_coef<T><<<(unsigned)((g.Nn + 255) / 256), 256, 0, st>>>(g, c0, nc);
+}
+template void qms_launch_node_coef<float>(const QGrid&, const QCoef<float>&, float*, cudaStream_t);
+template void qms_launch_node_coef<double>(const QGrid&, const QCoef<double>&, double*, cudaStream_t);
 
 void qms_launch_diag(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st) {
     qk_diag<<<op_grid(g), op_block(), 0, st>>>(g, c, P, dg);

@@ -226,24 +226,30 @@ __global__ void qk_ir_update(long long n, const T* __restrict__ e, const double*
 #define GM_MAXM 32
 struct GmPtrs { const void* p[GM_MAXM + 1]; };
 
-// block partials of V_i . w for i = 0..j (classical Gram-Schmidt projections)
-template <typename T>
-__global__ void qk_gm_dots(long long n, int j, GmPtrs V, const T* __restrict__ w, double* __restrict__ part) {
-    float acc[GM_MAXM];
+// block partials of V_i . w for i = 0..NV-1 (classical Gram-Schmidt projections).
+// NV is a compile-time count so every load of the unrolled loop is unconditional
+// and independent (memory-level parallelism over all basis vectors).
+template <typename T, int NV>
+__global__ void __launch_bounds__(256) qk_gm_dots(long long n, GmPtrs V, const T* __restrict__ w,
+                                                  double* __restrict__ part) {
+    float acc[NV];
 #pragma unroll
-    for (int i = 0; i < GM_MAXM; i++) acc[i] = 0.f;
+    for (int i = 0; i < NV; i++) acc[i] = 0.f;
+    const T* vp[NV];
+#pragma unroll
+    for (int i = 0; i < NV; i++) vp[i] = (const T*)V.p[i];
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         const float wv = (float)w[t];
+        T vv[NV];
 #pragma unroll
-        for (int i = 0; i < GM_MAXM; i++)
-            if (i <= j) acc[i] += (float)((const T*)V.p[i])[t] * wv;
+        for (int i = 0; i < NV; i++) vv[i] = __ldg(vp[i] + t);
+#pragma unroll
+        for (int i = 0; i < NV; i++) acc[i] += (float)vv[i] * wv;
     }
     __shared__ double sh[32];
-    for (int i = 0; i <= j; i++) {
-        float a = 0.f;
 #pragma unroll
-        for (int q = 0; q < GM_MAXM; q++) if (q == i) a = acc[q];
-        double sum = qBlockSum(a, sh);
+    for (int i = 0; i < NV; i++) {
+        double sum = qBlockSum(acc[i], sh);
         if (threadIdx.x == 0) part[(long long)i * gridDim.x + blockIdx.x] = sum;
     }
 }
@@ -259,19 +265,22 @@ __global__ void qk_gm_hcol(const double* __restrict__ part, long long nb, int j,
     }
 }
 
-// w -= sum_i h_ij V_i ; partials of |w|^2
-template <typename T>
-__global__ void qk_gm_orth(long long n, int j, int m, GmPtrs V, const double* __restrict__ Hm, T* __restrict__ w,
-                           double* __restrict__ part) {
-    T h[GM_MAXM];
+// w -= sum_i h_ij V_i ; partials of |w|^2   (NV = j + 1, compile-time)
+template <typename T, int NV>
+__global__ void __launch_bounds__(256) qk_gm_orth(long long n, int j, int m, GmPtrs V, const double* __restrict__ Hm,
+                                                  T* __restrict__ w, double* __restrict__ part) {
+    T h[NV];
+    const T* vp[NV];
 #pragma unroll
-    for (int i = 0; i < GM_MAXM; i++) h[i] = i <= j ? (T)Hm[i * m + j] : T(0);
+    for (int i = 0; i < NV; i++) { h[i] = (T)Hm[i * m + j]; vp[i] = (const T*)V.p[i]; }
     float acc = 0.f;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        T vv[NV];
+#pragma unroll
+        for (int i = 0; i < NV; i++) vv[i] = __ldg(vp[i] + t);
         T wv = w[t];
 #pragma unroll
-        for (int i = 0; i < GM_MAXM; i++)
-            if (i <= j) wv -= h[i] * ((const T*)V.p[i])[t];
+        for (int i = 0; i < NV; i++) wv -= h[i] * vv[i];
         w[t] = wv;
         acc += (float)(wv * wv);
     }
@@ -345,41 +354,60 @@ __global__ void qk_gm_solve(int k, int m, const double* __restrict__ Hm, double*
     }
 }
 
-// x += ||r|| * sum_i y_i Z_i   (FP64 accumulation of the refinement)
-template <typename T>
-__global__ void qk_gm_update(long long n, int k, int m, GmPtrs Z, const double* __restrict__ Gm,
-                             const double* __restrict__ S, double* __restrict__ x) {
+// x += sign * nrm * sum_i y_i Z_i   (FP64 accumulation of the refinement; sign -1 undoes it)
+template <typename T, int NV>
+__global__ void __launch_bounds__(256) qk_gm_update(long long n, int m, GmPtrs Z, const double* __restrict__ Gm,
+                                                    const double* __restrict__ S, double nrm_host, double sign,
+                                                    double* __restrict__ x) {
     const double* yv = Gm + 8 + 3 * m + 1;
-    T y[GM_MAXM];
+    T y[NV];
+    const T* zp[NV];
 #pragma unroll
-    for (int i = 0; i < GM_MAXM; i++) y[i] = i < k ? (T)yv[i] : T(0);
-    const double nr = S[S_NRM];
+    for (int i = 0; i < NV; i++) { y[i] = (T)yv[i]; zp[i] = (const T*)Z.p[i]; }
+    const double nr = sign * (S ? S[S_NRM] : nrm_host);
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        T zz[NV];
+#pragma unroll
+        for (int i = 0; i < NV; i++) zz[i] = __ldg(zp[i] + t);
         T acc = T(0);
 #pragma unroll
-        for (int i = 0; i < GM_MAXM; i++)
-            if (i < k) acc += y[i] * ((const T*)Z.p[i])[t];
+        for (int i = 0; i < NV; i++) acc += y[i] * zz[i];
         x[t] += nr * (double)acc;
     }
 }
 
-// x -= ||r_prev|| * e  (undo a refinement correction that increased the residual)
+// compile-time dispatch on the number of basis vectors (1..GM_MAXM)
+#define GM_CASES(M) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11) M(12) M(13) M(14) M(15) M(16) \
+    M(17) M(18) M(19) M(20) M(21) M(22) M(23) M(24) M(25) M(26) M(27) M(28) M(29) M(30) M(31) M(32)
+
 template <typename T>
-__global__ void qk_ir_revert_gm(long long n, int k, int m, GmPtrs Z, const double* __restrict__ Gm, double nrm,
-                                double* __restrict__ x) {
-    const double* yv = Gm + 8 + 3 * m + 1;
-    T y[GM_MAXM];
-#pragma unroll
-    for (int i = 0; i < GM_MAXM; i++) y[i] = i < k ? (T)yv[i] : T(0);
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        T acc = T(0);
-#pragma unroll
-        for (int i = 0; i < GM_MAXM; i++)
-            if (i < k) acc += y[i] * ((const T*)Z.p[i])[t];
-        x[t] -= nrm * (double)acc;
+static void gm_dots(int nv, int vb, cudaStream_t st, long long n, const GmPtrs& V, const T* w, double* part) {
+    switch (nv) {
+#define C(N) case N: qk_gm_dots<T, N><<<vb, 256, 0, st>>>(n, V, w, part); break;
+        GM_CASES(C)
+#undef C
+    }
+}
+template <typename T>
+static void gm_orth(int nv, int vb, cudaStream_t st, long long n, int j, int m, const GmPtrs& V, const double* Hm, T* w,
+                    double* part) {
+    switch (nv) {
+#define C(N) case N: qk_gm_orth<T, N><<<vb, 256, 0, st>>>(n, j, m, V, Hm, w, part); break;
+        GM_CASES(C)
+#undef C
+    }
+}
+template <typename T>
+static void gm_update(int nv, int vb, cudaStream_t st, long long n, int m, const GmPtrs& Z, const double* Gm,
+                      const double* S, double nrm, double sign, double* x) {
+    switch (nv) {
+#define C(N) case N: qk_gm_update<T, N><<<vb, 256, 0, st>>>(n, m, Z, Gm, S, nrm, sign, x); break;
+        GM_CASES(C)
+#undef C
     }
 }
 
+// x -= ||r_prev|| * e  (undo a refinement correction that increased the residual)
 template <typename T>
 __global__ void qk_ir_revert(long long n, const T* __restrict__ e, double nrm, double* __restrict__ x) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
@@ -429,15 +457,19 @@ void QmsSolver::release() {
     if (gm_H) cudaFree(gm_H);
     if (gm_scal) cudaFree(gm_scal);
     gm_H = gm_scal = nullptr;
-    void* ptrs[] = {ids, dtab64, dtab32, x, b, r64, H, slicebuf, part, S, status, dg_steady, dg_tr, mgtmp};
+    void* ptrs[] = {ids, dtab64, dtab32, x, b, r64, H, slicebuf, part, S, status, dg_steady, dg_tr, mgtmp, nc32, nc64};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
     for (auto& e : evpool) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     evpool.clear();
+    for (auto& e : graph_ev) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    graph_ev.clear();
     if (st && own_stream) cudaStreamDestroy(st);
     ids = nullptr; dtab64 = nullptr; dtab32 = nullptr; x = b = r64 = H = slicebuf = part = S = nullptr;
     status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr;
+    nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
 
@@ -448,6 +480,8 @@ int QmsSolver::init(const qms_desc& d) {
     if (d.xs < 4 || d.ys < 4 || d.zs < 4) { err = "grid must have at least 4 cells per axis"; return QMS_ERR_ARG; }
     if (!(d.dx > 0 && d.dy > 0 && d.dz > 0 && d.dt > 0)) { err = "dx, dy, dz, dt must be positive"; return QMS_ERR_ARG; }
     g = qms_make_grid(d.xs, d.ys, d.zs, d.dx, d.dy, d.dz);
+    // the stencil kernels index rows with 32-bit integers
+    if (g.n >= 0x7fffffffLL) { err = "grid too large: more than 2^31 - 1 unknowns"; return QMS_ERR_ARG; }
     fp64_inner = d.precision == QMS_PREC_FP64;
     tsize = fp64_inner ? sizeof(double) : sizeof(float);
     int nsm = 0;
@@ -461,7 +495,7 @@ int QmsSolver::init(const qms_desc& d) {
     own_stream = true;
     const long long n = g.n, ncell = (long long)g.xs * g.ys * g.zs;
     CK(cudaMalloc(&ids, ncell));
-    CK(cudaMemset(ids, 0, ncell));
+    CK(cudaMemsetAsync(ids, 0, ncell, st));
     CK(cudaMalloc(&dtab64, sizeof(QMatTable<double>)));
     CK(cudaMalloc(&dtab32, sizeof(QMatTable<float>)));
     CK(cudaMalloc(&x, n * 8));
@@ -472,9 +506,11 @@ int QmsSolver::init(const qms_desc& d) {
     CK(cudaMalloc(&slicebuf, 3 * smax * 8));
     CK(cudaMalloc(&part, npart * 8));
     CK(cudaMalloc(&S, S_COUNT * 8));
-    CK(cudaMemset(S, 0, S_COUNT * 8));
+    CK(cudaMemsetAsync(S, 0, S_COUNT * 8, st));
     CK(cudaMalloc(&status, sizeof(unsigned)));
-    CK(cudaMemset(status, 0, sizeof(unsigned)));
+    CK(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+    CK(cudaMalloc(&nc32, 6 * g.Nn * 4));
+    CK(cudaMalloc(&nc64, 6 * g.Nn * 8));
     CK(cudaMalloc(&dg_steady, n * 4));
     CK(cudaMalloc(&dg_tr, n * 4));
     for (auto& p : vec) CK(cudaMalloc(&p, n * tsize));
@@ -489,7 +525,7 @@ int QmsSolver::init(const qms_desc& d) {
         CK(cudaMalloc(&gm_scal, (size_t)(8 + 4 * m + 8) * 8));
     }
     CK(cudaMallocHost(&hS, S_COUNT * 8));
-    CK(cudaMemset(x, 0, n * 8));
+    CK(cudaMemsetAsync(x, 0, n * 8, st));
     double vac[6] = {1, 1, 1, 0, 0, 0};
     return set_materials(nullptr, vac, 0);
 }
@@ -501,13 +537,17 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
     return ncell + sizeof(QMatTable<double>) + sizeof(QMatTable<float>) + 3 * g.n * 8 + 3 * ncell * 8 +
+           6 * g.Nn * 12 +
            3 * smax * 8 + (4 * nb + 64) * 8 + 2 * g.n * 4 + (QMS_NVEC + 1) * g.n * ts + 4096 +
            (d.krylov == QMS_KRYLOV_GMRES ? (size_t)(2 * d.gmres_m + 1) * g.n * ts : 0) +
-           (d.precond == QMS_PRECOND_MG ? 2 * (ts == 8 ? QmsMG<double>::bytes_for(g, 5) : QmsMG<float>::bytes_for(g, 5)) : 0);
+           (d.precond == QMS_PRECOND_MG ? 2 * (ts == 8 ? QmsMG<double>::bytes_for(g, 5, true) : QmsMG<float>::bytes_for(g, 5, true)) : 0);
 }
 
 int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int nmat) {
     CK(cudaSetDevice(dev));
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    gm_k_est = 0;
+    gm_k_seen = 0;
     if (nmat < 0 || nmat > QMS_MAX_SLOTS - 1) { err = "nmat must be in 0..255"; return QMS_ERR_ARG; }
     const long long ncell = (long long)g.xs * g.ys * g.zs;
     if (host_slots) {
@@ -519,7 +559,9 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     qms_fill_table(htab32, rows6, nmat);
     CK(cudaMemcpyAsync(dtab64, &htab64, sizeof(htab64), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dtab32, &htab32, sizeof(htab32), cudaMemcpyHostToDevice, st));
-    // Jacobi diagonals of the steady and transient operators (velocity does not enter the diagonal)
+    // node coefficients, then the Jacobi diagonals (velocity does not enter the diagonal)
+    qms_launch_node_coef<float>(g, coef32(), nc32, st);
+    qms_launch_node_coef<double>(g, coef64(), nc64, st);
     QCoef<float> c32 = coef32();
     qms_launch_diag(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
     qms_launch_diag(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
@@ -545,8 +587,8 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     return 0;
 }
 
-QCoef<float> QmsSolver::coef32() const { return QCoef<float>{g, ids, dtab32, (float)(1.0 / QMS_MU0)}; }
-QCoef<double> QmsSolver::coef64() const { return QCoef<double>{g, ids, dtab64, 1.0 / QMS_MU0}; }
+QCoef<float> QmsSolver::coef32() const { return QCoef<float>{g, ids, dtab32, (float)(1.0 / QMS_MU0), nc32}; }
+QCoef<double> QmsSolver::coef64() const { return QCoef<double>{g, ids, dtab64, 1.0 / QMS_MU0, nc64}; }
 
 int QmsSolver::finalize(int fop, int nsum, long long nb) {
     qk_finalize<<<1, 512, 0, st>>>(part, nb, nsum, S, fop, status);
@@ -562,7 +604,7 @@ void QmsSolver::op(bool adv, int mode, const QStepPar<T>& P, const T* xin, const
                           (double)g.n * sizeof(T) * (2 + (w && w != xin ? 1 : 0) + (bin ? 1 : 0)) + ncell);
     qms_launch_operator<T>(g, coef<T>(), P, adv, mode, xin, bin, y, w, partials, st);
     nlaunch++;
-    if (ev) cudaEventRecord(ev->b, st);
+    prof_end(ev);
 }
 template void QmsSolver::op<float>(bool, int, const QStepPar<float>&, const float*, const float*, float*,
                                    const float*, double*);
@@ -580,8 +622,25 @@ QmsSolver::OpEv* QmsSolver::prof_begin(int kind, double bytes) {
     OpEv* ev = &evpool[evused++];
     ev->kind = kind;
     ev->bytes = bytes;
-    cudaEventRecord(ev->a, st);
+    // inside a capture the record must become an event-record node of the graph
+    cudaEventRecordWithFlags(ev->a, st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     return ev;
+}
+
+void QmsSolver::prof_end(OpEv* ev) {
+    if (ev) cudaEventRecordWithFlags(ev->b, st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
+}
+
+bool QmsSolver::prof_accum(const OpEv& e) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, e.a, e.b) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (e.kind == 1) { profacc.op64_launches++; profacc.op64_ms += ms; profacc.op64_bytes += e.bytes; }
+    else if (e.kind == 0) { profacc.op32_launches++; profacc.op32_ms += ms; profacc.op32_bytes += e.bytes; }
+    else { profacc.mg_cycles++; profacc.mg_ms += ms; }
+    return true;
 }
 
 int QmsSolver::profile_enable(bool on) {
@@ -597,13 +656,8 @@ int QmsSolver::profile_enable(bool on) {
 
 int QmsSolver::profile_collect(qms_profile* out) {
     CK(cudaStreamSynchronize(st));
-    for (size_t q = 0; q < evused; q++) {
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, evpool[q].a, evpool[q].b));
-        if (evpool[q].kind == 1) { profacc.op64_launches++; profacc.op64_ms += ms; profacc.op64_bytes += evpool[q].bytes; }
-        else if (evpool[q].kind == 0) { profacc.op32_launches++; profacc.op32_ms += ms; profacc.op32_bytes += evpool[q].bytes; }
-        else { profacc.mg_cycles++; profacc.mg_ms += ms; }
-    }
+    for (size_t q = 0; q < evused; q++)
+        if (!prof_accum(evpool[q])) { err = "profile events could not be timed"; return QMS_ERR_CUDA; }
     evused = 0;
     profacc.launches = nlaunch;
     *out = profacc;
@@ -624,7 +678,7 @@ void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool
             nlaunch += mgf[transient ? 1 : 0].vcycle((const float*)r, bscale, (float*)z, (float*)mgtmp, mask_v, st);
         else
             nlaunch += mgd[transient ? 1 : 0].vcycle((const double*)r, bscale, (double*)z, (double*)mgtmp, mask_v, st);
-        if (ev) cudaEventRecord(ev->b, st);
+        prof_end(ev);
     } else if (jacobi_pcg) {
         qk_jacobi<T><<<(int)vec_blocks, 256, 0, st>>>(g.n, mask_v ? g.oV : g.n, r, transient ? dg_tr : dg_steady, z);
         nlaunch++;
@@ -667,7 +721,8 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
             if (rc) return rc;
             if (!(hS[S_RR] <= tol2 * hS[S_RR0])) {
                 unsigned stt = 0;
-                CK(cudaMemcpy(&stt, status, 4, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpyAsync(&stt, status, 4, cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
                 if (stt & QMS_ST_BREAKDOWN) break;
                 continue;
             }
@@ -682,9 +737,10 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
 
 
 template <typename T>
-int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& iters) {
+int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& iters, int fixed_k) {
     const long long n = g.n;
     const int m = std::min(desc.gmres_m, GM_MAXM);
+    const int kmax = fixed_k > 0 ? std::min(fixed_k, m) : m;
     const float* dg = transient ? dg_tr : dg_steady;
     QStepPar<T> P = qms_step_par<T>(g, v[0], v[1], v[2], desc.dt, transient);
     const int vb = (int)vec_blocks;
@@ -697,26 +753,26 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
     nlaunch += 2;
     const double tol = desc.inner_rtol;
     int k = 0;
-    for (int j = 0; j < m; j++) {
+    for (int j = 0; j < kmax; j++) {
         T* vj = (T*)gmV[j];
         T* zj = use_mg ? (T*)gmZ[j] : vj;
         if (use_mg) precond<T>(vj, dg, zj, false, transient, false);
         op<T>(adv, QOPH_SCALED, P, zj, nullptr, w, nullptr, nullptr);
-        qk_gm_dots<T><<<vb, 256, 0, st>>>(n, j, Vp, w, part);
+        gm_dots<T>(j + 1, vb, st, n, Vp, w, part);
         qk_gm_hcol<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H);
-        qk_gm_orth<T><<<vb, 256, 0, st>>>(n, j, m, Vp, gm_H, w, part);
+        gm_orth<T>(j + 1, vb, st, n, j, m, Vp, gm_H, w, part);
         qk_gm_givens<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H, gm_scal, status);
         qk_gm_scale<T><<<vb, 256, 0, st>>>(n, w, (T*)gmV[j + 1], gm_scal);
         nlaunch += 5;
         k = j + 1;
-        if ((j + 1) % desc.check_every == 0 || j + 1 == m) {
+        if (fixed_k <= 0 && ((j + 1) % desc.check_every == 0 || j + 1 == m)) {
             CK(cudaMemcpyAsync(hS, gm_scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             if (!(hS[1] > tol * hS[0])) break;       // also stops on a non-finite estimate
         }
     }
     qk_gm_solve<<<1, 32, 0, st>>>(k, m, gm_H, gm_scal);
-    qk_gm_update<T><<<vb, 256, 0, st>>>(n, k, m, Zp, gm_scal, S, x);
+    gm_update<T>(k, vb, st, n, m, Zp, gm_scal, S, 0.0, 1.0, x);
     nlaunch += 2;
     last_gm_k = k;
     iters = k;
@@ -731,7 +787,7 @@ void QmsSolver::revert_last(double nrm) {
         const int m = std::min(desc.gmres_m, GM_MAXM);
         GmPtrs Zp{};
         for (int i = 0; i < m; i++) Zp.p[i] = use_mg ? gmZ[i] : gmV[i];
-        qk_ir_revert_gm<T><<<vb, 256, 0, st>>>(g.n, last_gm_k, m, Zp, gm_scal, nrm, x);
+        gm_update<T>(last_gm_k, vb, st, g.n, m, Zp, gm_scal, nullptr, nrm, -1.0, x);
     } else {
         qk_ir_revert<T><<<vb, 256, 0, st>>>(g.n, (const T*)vec[6], nrm, x);
     }
@@ -778,12 +834,68 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
     return 0;
 }
 
-int QmsSolver::residual(bool adv, bool transient, const double v[3]) {
+void QmsSolver::residual_launch(bool adv, bool transient, const double v[3]) {
     QStepPar<double> P = qms_step_par<double>(g, v[0], v[1], v[2], desc.dt, transient);
     op<double>(adv, QOPH_RESID, P, x, b, r64, nullptr, part);
     finalize(FIN_RESID, 4, nbop);
+}
+
+int QmsSolver::residual(bool adv, bool transient, const double v[3]) {
+    residual_launch(adv, transient, v);
     CK(cudaGetLastError());
     return read_scalars();
+}
+
+// One refinement iteration (FGMRES with k iterations, FP64 update, FP64 residual) as a
+// CUDA graph, captured once per (velocity, form, k) and replayed.
+int QmsSolver::ir_iteration_graph(bool adv, bool transient, const double v[3], int k) {
+    const bool want_prof = prof && !graph_prof_broken;
+    const bool same = graph_exec && graph_k == k && graph_tr == transient && graph_adv == adv &&
+                      graph_v[0] == v[0] && graph_v[1] == v[1] && graph_v[2] == v[2] && graph_prof == want_prof;
+    if (!same) {
+        if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+        // with profiling on, the operator / V-cycle event records are captured as graph nodes
+        // on their own event set and read back after every replay
+        const bool prof_was = prof;
+        const size_t ev_saved = evused;
+        prof = want_prof;
+        std::swap(evpool, graph_ev);
+        evused = 0;
+        capturing = true;
+        const long long n0 = nlaunch;
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        int rc = 0;
+        if (e == cudaSuccess) {
+            int it = 0;
+            rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it, k) : inner_gmres<float>(adv, transient, v, it, k);
+            residual_launch(adv, transient, v);
+        }
+        cudaGraph_t graph = nullptr;
+        if (e == cudaSuccess) e = cudaStreamEndCapture(st, &graph);
+        capturing = false;
+        graph_evn = evused;
+        std::swap(evpool, graph_ev);
+        evused = ev_saved;
+        prof = prof_was;
+        if (rc) return rc;
+        if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return QMS_ERR_CUDA; }
+        e = cudaGraphInstantiate(&graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { err = std::string("graph instantiate: ") + cudaGetErrorString(e); return QMS_ERR_CUDA; }
+        graph_launches = nlaunch - n0;
+        nlaunch = n0;
+        graph_k = k; graph_tr = transient; graph_adv = adv; graph_prof = want_prof;
+        graph_v[0] = v[0]; graph_v[1] = v[1]; graph_v[2] = v[2];
+    }
+    CK(cudaGraphLaunch(graph_exec, st));
+    nlaunch += graph_launches;
+    last_inner = 2;
+    last_gm_k = k;
+    int rc = read_scalars();                     // synchronises the stream
+    if (rc == 0 && graph_prof && prof)
+        for (size_t q = 0; q < graph_evn; q++)
+            if (!prof_accum(graph_ev[q])) { graph_prof_broken = true; break; }
+    return rc;
 }
 
 int QmsSolver::solve(bool transient, const double v[3], const double B[3], const double G[9]) {
@@ -800,9 +912,16 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     stats = qms_stats{};
     double rel = INFINITY, prev_rn = INFINITY, sref = 0.0;
     int outer = 0, stalled = 0;
+    graph_resid_ready = false;
+    const int gm_m = std::min(desc.gmres_m, GM_MAXM);
+    int graph_k_used = 0;                 // k of the graph replay that produced this residual (0: none)
     for (;;) {
-        int rc = residual(adv, transient, v);
-        if (rc) return rc;
+        int rc = 0;
+        if (!graph_resid_ready) {
+            rc = residual(adv, transient, v);
+            if (rc) return rc;
+        }
+        graph_resid_ready = false;
         const double xn = std::sqrt(hS[S_XA] + hS[S_XV]);
         const double rn = std::sqrt(hS[S_RA] + hS[S_RV]);
         // The scale is fixed by the state at the start of the solve (the previous step, or the
@@ -814,8 +933,21 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         if (outer == 0) stats.initial_residual = rel;
         if (!std::isfinite(rel)) { stats.status |= QMS_ST_NAN; break; }
         if (rel <= desc.tol || rn == 0.0) break;
+        // A replayed iteration runs a fixed number k of FGMRES steps.  If it missed the inner
+        // target, raise k for the next replay to what the observed per-step rate needs
+        // (k log(target) / log(rho)); such a miss is not a stall while k can still grow.
+        bool k_limited = false;
+        if (graph_k_used > 0 && prev_rn > 0 && rn > 0 && rn < prev_rn) {
+            const double rho = rn / prev_rn;
+            if (rho > desc.inner_rtol && graph_k_used < gm_m) {
+                const double need = graph_k_used * std::log(desc.inner_rtol) / std::log(std::min(rho, 0.999));
+                gm_k_est = std::min(gm_m, std::max(graph_k_used + 1, (int)std::ceil(need)));
+                k_limited = true;
+            }
+        }
+        graph_k_used = 0;
         // refinement at the round-off floor: two iterations without halving the residual
-        stalled = rn > 0.5 * prev_rn ? stalled + 1 : 0;
+        stalled = rn > 0.5 * prev_rn && !k_limited ? stalled + 1 : 0;
         if (stalled >= 2) {
             if (rel > 1e3 * desc.tol) stats.status |= QMS_ST_NO_CONVERGENCE;
             break;
@@ -839,14 +971,27 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
             last_inner = 1;
             rc = fp64_inner ? inner_bicgstab<double>(adv, transient, v, it)
                             : inner_bicgstab<float>(adv, transient, v, it);
+        } else if (desc.use_graphs && gm_k_est > 0) {
+            // replay the captured refinement iteration; its residual is read back with it
+            it = gm_k_est;
+            rc = ir_iteration_graph(adv, transient, v, gm_k_est);
+            if (rc) return rc;
+            graph_k_used = it;
+            stats.inner_iterations += it;
+            outer++;
+            graph_resid_ready = true;
+            continue;
         } else {
             last_inner = 2;
-            rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it) : inner_gmres<float>(adv, transient, v, it);
+            rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it, 0) : inner_gmres<float>(adv, transient, v, it, 0);
+            if (!rc) gm_k_seen = std::max(gm_k_seen, it);
         }
         if (rc) return rc;
         stats.inner_iterations += it;
         outer++;
     }
+    if (!use_cg && desc.krylov == QMS_KRYLOV_GMRES && desc.use_graphs && gm_k_est == 0 && gm_k_seen > 0)
+        gm_k_est = std::min(std::min(desc.gmres_m, GM_MAXM), gm_k_seen + 1);
     unsigned stt = 0;
     CK(cudaMemcpyAsync(&stt, status, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -880,8 +1025,8 @@ template int QmsSolver::inner_bicgstab<float>(bool, bool, const double*, int&);
 template int QmsSolver::inner_bicgstab<double>(bool, bool, const double*, int&);
 template int QmsSolver::inner_pcg<float>(bool, int&);
 template int QmsSolver::inner_pcg<double>(bool, int&);
-template int QmsSolver::inner_gmres<float>(bool, bool, const double*, int&);
-template int QmsSolver::inner_gmres<double>(bool, bool, const double*, int&);
+template int QmsSolver::inner_gmres<float>(bool, bool, const double*, int&, int);
+template int QmsSolver::inner_gmres<double>(bool, bool, const double*, int&, int);
 template void QmsSolver::revert_last<float>(double);
 template void QmsSolver::revert_last<double>(double);
 template void QmsSolver::precond<float>(const float*, const float*, float*, bool, bool, bool);

@@ -36,6 +36,8 @@ struct QmsSolver {
     double* S = nullptr;        // device scalars
     double* hS = nullptr;       // pinned host mirror
     unsigned* status = nullptr;
+    float* nc32 = nullptr;      // node coefficients (6 x Nn), FP32 and FP64
+    double* nc64 = nullptr;
     float* dg_steady = nullptr; // Jacobi diagonals
     float* dg_tr = nullptr;
     void* vec[QMS_NVEC] = {};   // inner Krylov vectors (FP32 or FP64)
@@ -55,8 +57,14 @@ struct QmsSolver {
     long long nlaunch = 0;
     struct OpEv { cudaEvent_t a, b; int kind; double bytes; };   // kind: 0 op32, 1 op64, 2 V-cycle
     OpEv* prof_begin(int kind, double bytes);
+    void prof_end(OpEv* ev);
+    bool prof_accum(const OpEv& e);              // false when the events cannot be timed
     std::vector<OpEv> evpool;
     size_t evused = 0;
+    bool capturing = false;                      // event records go into a graph being captured
+    std::vector<OpEv> graph_ev;                  // event records inside the captured graph
+    size_t graph_evn = 0;
+    bool graph_prof = false, graph_prof_broken = false;
     qms_profile profacc{};
     int profile_enable(bool on);
     int profile_collect(qms_profile* out);
@@ -79,7 +87,17 @@ struct QmsSolver {
 
     template <typename T> int inner_bicgstab(bool adv, bool transient, const double v[3], int& iters);
     template <typename T> int inner_pcg(bool transient, int& iters);
-    template <typename T> int inner_gmres(bool adv, bool transient, const double v[3], int& iters);
+    template <typename T> int inner_gmres(bool adv, bool transient, const double v[3], int& iters, int fixed_k);
+    void residual_launch(bool adv, bool transient, const double v[3]);
+    int ir_iteration_graph(bool adv, bool transient, const double v[3], int k);
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_k = 0;
+    bool graph_tr = false, graph_adv = false;
+    double graph_v[3] = {0, 0, 0};
+    long long graph_launches = 0;
+    bool graph_resid_ready = false;
+    int gm_k_est = 0;           // FGMRES iterations replayed per refinement iteration (0: not yet known)
+    int gm_k_seen = 0;          // largest count seen while running with host checks
     template <typename T> void revert_last(double nrm);
     void* gmV[33] = {};         // FGMRES basis (m + 1) and preconditioned directions (m)
     void* gmZ[32] = {};

@@ -218,9 +218,15 @@ def latency_report(results: List[SolveResult], wall: float) -> Dict:
 
     def pct(a, p):
         return float(np.percentile(a, p)) if a.size else None
+    errors: Dict[str, int] = {}
+    for r in results:
+        if r.status != "ok":
+            key = r.error[:200]
+            errors[key] = errors.get(key, 0) + 1
     return {"requests": len(results), "completed": len(ok),
             "failed": sum(r.status == "failed" for r in results),
             "rejected": sum(r.status == "rejected" for r in results),
+            "errors": errors,
             "step_p50_ms": 1e3 * pct(steps, 50) if steps.size else None,
             "step_p99_ms": 1e3 * pct(steps, 99) if steps.size else None,
             "request_p50_s": pct(req, 50), "request_p99_s": pct(req, 99),

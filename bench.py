@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--cpu-steps", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 step comparison")
     ap.add_argument("--check-every", type=int, default=None)
     return ap.parse_args()
 
@@ -276,6 +277,35 @@ def run_gpu(args):
         e2e = {"value": e2e_units / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 15 * 8,
                "d2h_bytes_per_step": slice_bytes}
 
+    # Accuracy at the bench workload: one more step in both precisions from the same state,
+    # compared per unknown block (A, V) and on H, the field the reference dumps.
+    accuracy = None
+    if not args.no_accuracy and rank == 0 and args.precision == "mixed":
+        x_prev = solver.get_state()
+        counter += 1
+        v = sched.step(counter)
+        solver.step(v, B, G)
+        xm = solver.get_state()
+        hm = [h.copy() for h in solver.fields()]
+        s64 = QMSSolver(default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt, precision="fp64",
+                                     device=local))
+        s64.set_geometry_f64(geom, inp.props_table())
+        s64.set_state(x_prev)
+        st64 = s64.step(v, B, G)
+        xd = s64.get_state()
+        hd = s64.fields()
+        oV = n - (inp.xs + 1) * (inp.ys + 1) * (inp.zs + 1)
+
+        def rel(a, b):
+            nb = float(np.linalg.norm(b))
+            return float(np.linalg.norm(a - b)) / nb if nb > 0 else float(np.linalg.norm(a))
+        accuracy = {"vs": "fp64 GPU solver, same start state, one step", "step": counter,
+                    "rel_l2_A": rel(xm[:oV], xd[:oV]), "rel_l2_V": rel(xm[oV:], xd[oV:]),
+                    "rel_l2_H": rel(np.concatenate([h.ravel() for h in hm]), np.concatenate([h.ravel() for h in hd])),
+                    "fp64_iters": {"outer": st64["outer"], "inner": st64["inner"]}}
+        accuracy["pass_1e-8"] = all(accuracy[k] <= 1e-8 for k in ("rel_l2_A", "rel_l2_V", "rel_l2_H"))
+        s64.close()
+
     peak, peak_kind = measured_peak()
     kern = "qk_operator_f32" if prof["op32_ms"] >= prof["op64_ms"] else "qk_operator_f64_resid"
     kms = prof["op32_ms"] if kern == "qk_operator_f32" else prof["op64_ms"]
@@ -310,6 +340,7 @@ def run_gpu(args):
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                            "l2": "inputs larger than L2 (one FP32 vector = %.0f MB)" % (n * 4 / 1e6)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": prof["launches"],
+                "accuracy": accuracy,
                 "clocks": clk, "steady_s": steady_s,
                 "steady_iters": {"outer": st0["outer"], "inner": st0["inner"]},
                 "step_iters": [{"outer": s["outer"], "inner": s["inner"], "r": s["r"]} for s in iters]}

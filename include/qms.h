@@ -90,6 +90,8 @@ typedef struct {
                                 potential of isolated conductors) */
     int krylov;              /* nonsymmetric inner solver: QMS_KRYLOV_GMRES (default) or _BICGSTAB */
     int gmres_m;             /* FGMRES basis size per refinement iteration (<= 32) */
+    int use_graphs;          /* replay each refinement iteration of a step as one CUDA graph, with the
+                                FGMRES iteration count learned from the first solve (1 = on) */
 } qms_desc;
 
 typedef struct {

@@ -248,3 +248,30 @@ def test_dropin_dumps_vs_reference_program(name, tmp_path):
             a = np.concatenate([got[q][rec] for q in range(3)])
             b = np.concatenate([ref[q][rec] for q in range(3)])
             assert rel_l2(a, b, floor=1e-30) <= 1e-8, (group[0], rec, rel_l2(a, b))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_plain_block_32_twenty_steps(precision):
+    """The 32^3 copper block under a 1 kHz field (steady + 20 steps): every z-mid H
+    slice record within 1e-8 relative L2 of the oracle's direct solve
+    (tests/golden/plain_block_32.npz, made by tests/golden/make_config1.py)."""
+    from alpineqms_gb300 import workloads
+    from alpineqms_gb300.trajectory import VelocitySchedule, scaled_field
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "plain_block_32.npz"))
+    inp, geom = workloads.plain_block_32()
+    sched = VelocitySchedule(inp.traj, inp.dt)
+    s = solver_for(inp.xs, inp.ys, inp.zs, (inp.dx, inp.dy, inp.dz), inp.dt, geom, inp.props_table(),
+                   precision=precision)
+    sl = int(z["slice_index"]) - 1
+    for n in range(0, inp.nt + 1):
+        B, G = scaled_field(inp.B, inp.G, inp.excitation, n * inp.dt)
+        st = s.steady(sched.steady(), B, G) if n == 0 else s.step(sched.step(n), B, G)
+        assert st["status"] == 0, (n, st)
+        H = s.fields()
+        got = np.stack([h.reshape((inp.xs, inp.ys, inp.zs), order="F")[:, :, sl] for h in H])
+        assert rel_l2(got, z["slices"][n]) <= 1e-8, (n, rel_l2(got, z["slices"][n]))
+        hn = np.sqrt(sum(np.dot(h.ravel(), h.ravel()) for h in H))
+        assert abs(hn - z["hnorm"][n]) <= 1e-8 * z["hnorm"][n], (n, hn, z["hnorm"][n])
+        xa = s.get_state()[:o.block_offsets(inp.xs, inp.ys, inp.zs)[3]]
+        assert abs(np.linalg.norm(xa) - z["anorm"][n]) <= 1e-8 * z["anorm"][n]
+    s.close()
