@@ -38,7 +38,7 @@ class QmsDesc(ctypes.Structure):
                 ("mg_vshift", ctypes.c_double),
                 ("krylov", ctypes.c_int),
                 ("gmres_m", ctypes.c_int),
-                ("use_graphs", ctypes.c_int)]
+                ("use_graphs", ctypes.c_int), ("mg_region_cut", ctypes.c_double)]
 
 
 class QmsStats(ctypes.Structure):
@@ -56,6 +56,43 @@ class QmsProfile(ctypes.Structure):
                 ("mg_cycles", ctypes.c_int64), ("mg_ms", ctypes.c_double)]
 
 
+class QmsSrvDesc(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_double), ("max_resident", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class QmsRequest(ctypes.Structure):
+    _fields_ = [("xs", ctypes.c_int), ("ys", ctypes.c_int), ("zs", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+                ("nt", ctypes.c_int), ("tt", ctypes.c_int), ("slice_axis", ctypes.c_int),
+                ("slice_index", ctypes.c_int), ("keep", ctypes.c_int), ("precision", ctypes.c_int),
+                ("B", ctypes.c_double * 3), ("G", ctypes.c_double * 9), ("traj", (ctypes.c_double * 3) * 3),
+                ("exc_kind", ctypes.c_int), ("exc_f", ctypes.c_double), ("exc_phase", ctypes.c_double),
+                ("geom", ctypes.c_void_p), ("table", ctypes.c_void_p), ("nmat", ctypes.c_int)]
+
+
+class QmsSrvResult(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("rc", ctypes.c_int), ("n_dims", ctypes.c_longlong),
+                ("steps_done", ctypes.c_int), ("arrival_s", ctypes.c_double), ("admitted_s", ctypes.c_double),
+                ("finished_s", ctypes.c_double), ("steady_s", ctypes.c_double), ("step_mean_s", ctypes.c_double),
+                ("step_max_s", ctypes.c_double), ("n_slice_values", ctypes.c_longlong)]
+
+
+class QmsSrvStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong), ("failed", ctypes.c_longlong),
+                ("rejected", ctypes.c_longlong), ("step_p50_ms", ctypes.c_double), ("step_p99_ms", ctypes.c_double),
+                ("request_p50_s", ctypes.c_double), ("request_p99_s", ctypes.c_double),
+                ("queue_wait_p50_s", ctypes.c_double), ("queue_wait_p99_s", ctypes.c_double),
+                ("dof_timesteps", ctypes.c_double), ("wall_s", ctypes.c_double), ("peak_bytes", ctypes.c_double),
+                ("peak_resident", ctypes.c_int)]
+
+
+# struct name in include/qms.h -> ctypes mirror (checked field by field by tests/test_capi_cpu.py)
+STRUCTS = {"qms_desc": None, "qms_stats": None, "qms_profile": None, "qms_srv_desc": QmsSrvDesc,
+           "qms_request": QmsRequest, "qms_srv_result": QmsSrvResult, "qms_srv_stats": QmsSrvStats}
+
+QMS_SRV_QUEUED, QMS_SRV_RUNNING, QMS_SRV_DONE, QMS_SRV_FAILED, QMS_SRV_REJECTED = range(5)
+QMS_KEEP_NONE, QMS_KEEP_SLICES = 0, 1
+QMS_EXC_NONE, QMS_EXC_COS, QMS_EXC_SIN = 0, 1, 2
 QMS_PREC_MIXED, QMS_PREC_FP64 = 0, 1
 QMS_FIELD_CUBES, QMS_FIELD_SLICE = 0, 1
 ERRORS = {-1: "QMS_ERR_ARG", -2: "QMS_ERR_CUDA", -3: "QMS_ERR_NOMEM", -4: "QMS_ERR_STATE", -5: "QMS_ERR_CONVERGE"}
@@ -91,7 +128,16 @@ SIGNATURES = [
     ("qms_residual_noalloc", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int, _DP, _VP, _VP,
                                                                                       ctypes.c_int, _VP, _VP, _VP,
                                                                                       _VP, _VP]),
+    ("qms_srv_create", ctypes.c_int, [ctypes.POINTER(QmsSrvDesc), ctypes.POINTER(_H)]),
+    ("qms_srv_submit", ctypes.c_int, [_H, ctypes.POINTER(QmsRequest), ctypes.POINTER(ctypes.c_longlong)]),
+    ("qms_srv_poll", ctypes.c_int, [_H, ctypes.c_longlong, ctypes.POINTER(QmsSrvResult)]),
+    ("qms_srv_wait", ctypes.c_int, [_H, ctypes.c_longlong, ctypes.POINTER(QmsSrvResult)]),
+    ("qms_srv_slices", ctypes.c_longlong, [_H, ctypes.c_longlong, _VP, ctypes.c_longlong]),
+    ("qms_srv_error", ctypes.c_char_p, [_H, ctypes.c_longlong]),
+    ("qms_srv_stats_get", ctypes.c_int, [_H, ctypes.POINTER(QmsSrvStats)]),
+    ("qms_srv_destroy", None, [_H]),
 ]
+STRUCTS.update({"qms_desc": QmsDesc, "qms_stats": QmsStats, "qms_profile": QmsProfile})
 
 
 def lib_path() -> str:

@@ -27,6 +27,7 @@ SOURCES = {
     "qms_mg.cu": [],
     "qms_noalloc.cu": [],
     "qms_capi.cu": [],
+    "qms_server.cpp": [],
 }
 
 
@@ -41,7 +42,7 @@ def _inputs_digest() -> str:
     h = hashlib.sha256()
     for d in (CSRC, INCLUDE):
         for fn in sorted(os.listdir(d)):
-            if fn.endswith((".cu", ".cuh", ".h")):
+            if fn.endswith((".cu", ".cuh", ".h", ".cpp")):
                 with open(os.path.join(d, fn), "rb") as f:
                     h.update(fn.encode() + f.read())
     h.update(repr(SOURCES).encode() + repr(ARCH).encode())
@@ -59,7 +60,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
             *(extra_flags or [])]
 
     def compile_one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = base + SOURCES[src] + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd))

@@ -36,7 +36,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->dx = dx; d->dy = dy; d->dz = dz; d->dt = dt;
     d->precision = QMS_PREC_MIXED;
     d->tol = 1e-12;
-    d->max_outer = 30;
+    d->max_outer = 60;
     d->max_inner = 500;
     d->inner_rtol = 1e-3;
     d->check_every = 2;
@@ -48,6 +48,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->krylov = QMS_KRYLOV_GMRES;
     d->gmres_m = 24;
     d->use_graphs = 1;
+    d->mg_region_cut = 0.0;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }

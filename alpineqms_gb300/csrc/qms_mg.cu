@@ -28,6 +28,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <vector>
 
 namespace {
@@ -324,7 +325,7 @@ __device__ __forceinline__ T mg_rcp(T d) {
 }
 
 template <typename T, int KIND>
-__global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __restrict__ b,
           const float* __restrict__ bscale, const T* __restrict__ xin, T* __restrict__ xout, MGLevelDev<T> C,
           T* __restrict__ bc) {
@@ -401,8 +402,11 @@ mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, con
                 return;
             }
             const T xc = XS(q, x0, 0, 0);
-            const T Ax = d * xc - wxp * XS(q, x0, 0, 1) - wxm * XS(q, x0, 0, -1) - wyp * XS(q, x0, 1, 0) -
-                         wym * XS(q, x0, -1, 0) - wzp * XS(q, xp, 0, 0) - wzm * XS(q, xm, 0, 0);
+            // difference form (rounding scales with the variation of x): d - sum(w) is the mass
+            // term, or the diagonal shift of V
+            const T Ax = wxp * (xc - XS(q, x0, 0, 1)) + wxm * (xc - XS(q, x0, 0, -1)) + wyp * (xc - XS(q, x0, 1, 0)) +
+                         wym * (xc - XS(q, x0, -1, 0)) + wzp * (xc - XS(q, xp, 0, 0)) + wzm * (xc - XS(q, xm, 0, 0)) +
+                         (dextra * dscale + (wxp + wxm + wyp + wym + wzp + wzm) * (dscale - T(1))) * xc;
             if (KIND == 2) r[q] = bv - Ax;
             else xout[row] = xc + omega * (bv - Ax) * mg_rcp(d);
         };
@@ -459,26 +463,22 @@ mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, con
 }
 
 // level 0: x += alpha P x_c on the active points (the Dirichlet points of every component,
-// and V when masked, stay zero); one thread per unknown
+// and V when masked, stay zero); one thread per node (i, j, k), its (up to) four unknowns
 template <typename T>
 __global__ void mg0_prolong(QGrid g, int mask_v, T* __restrict__ x, MGLevelDev<T> C, const T* __restrict__ xc,
                             T alpha) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n) return;
-    int q, n1, n2;
-    long long o;
-    if (t < g.oY) { q = 0; o = t; n1 = g.xs; n2 = g.Ny; }
-    else if (t < g.oZ) { q = 1; o = t - g.oY; n1 = g.Nx; n2 = g.ys; }
-    else if (t < g.oV) { q = 2; o = t - g.oZ; n1 = g.Nx; n2 = g.Ny; }
-    else { q = 3; o = t - g.oV; n1 = g.Nx; n2 = g.Ny; }
-    const int oi = (int)o;
-    const int i = oi % n1 + 1, j = (oi / n1) % n2 + 1, k = oi / (n1 * n2) + 1;
-    const bool fixed = q == 0 ? qFixX(g, i, j, k) : q == 1 ? qFixY(g, i, j, k) : q == 2 ? qFixZ(g, i, j, k)
-                                                                                   : (mask_v || qFixV(g, i, j, k));
-    if (fixed) return;                    // the sweeps keep these at zero
-    const MGBlockDesc& cb = C.blk[q];
-    x[t] += alpha * xc[cb.off + ((i - 1) >> 1) + (long long)((j - 1) >> 1) * cb.n1 +
-                       (long long)((k - 1) >> 1) * cb.n1 * cb.n2];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > g.Nx) return;
+    const int I = (i - 1) >> 1, J = (j - 1) >> 1, K = (k - 1) >> 1;
+    auto coarse = [&](int q) {
+        const MGBlockDesc& cb = C.blk[q];
+        return xc[cb.off + I + (long long)J * cb.n1 + (long long)K * cb.n1 * cb.n2];
+    };
+    const int sXk = g.xs * g.Ny, sYk = g.Nx * g.ys, sZk = g.Nx * g.Ny;
+    if (i <= g.xs && !qFixX(g, i, j, k)) x[(i - 1) + (j - 1) * g.xs + (k - 1) * sXk] += alpha * coarse(0);
+    if (j <= g.ys && !qFixY(g, i, j, k)) x[g.oY + (i - 1) + (j - 1) * g.Nx + (k - 1) * sYk] += alpha * coarse(1);
+    if (k <= g.zs && !qFixZ(g, i, j, k)) x[g.oZ + (i - 1) + (j - 1) * g.Nx + (k - 1) * sZk] += alpha * coarse(2);
+    if (!mask_v && !qFixV(g, i, j, k)) x[g.oV + (i - 1) + (j - 1) * g.Nx + (k - 1) * sZk] += alpha * coarse(3);
 }
 
 template <typename T, int KIND>
@@ -788,7 +788,7 @@ int QmsMG<T>::vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v
         T* t = l == 0 ? cur_t0 : L.t;
         if (l == 0 && tiled0) {
             // in place: level 0 then writes nu1 + nu2 times, alternating from the buffer chosen above
-            mg0_prolong<T><<<nblk(g0.n), 256, 0, st>>>(g0, mv, x, lv[1], lv[1].x, alpha);
+            mg0_prolong<T><<<dim3((g0.Nx + 127) / 128, g0.Ny, g0.Nz), 128, 0, st>>>(g0, mv, x, lv[1], lv[1].x, alpha);
         } else {
             // untiled: prolongate in place, or out of place when the parity of the nu2
             // sweeps would leave the level-0 result in the temporary
@@ -815,3 +815,262 @@ int QmsMG<T>::vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v
 
 template struct QmsMG<float>;
 template struct QmsMG<double>;
+
+// ---------------------------------------------------------------------------
+// conductor-region coarse space of the V block
+// ---------------------------------------------------------------------------
+namespace {
+
+// s[r] = sum over the V rows of region r of b * bscale (FP64, fixed order: one CTA per region)
+template <typename T>
+__global__ void qk_region_sums(const int* __restrict__ ptr, const int* __restrict__ rows, const T* __restrict__ b,
+                               const float* __restrict__ bscale, double* __restrict__ s) {
+    __shared__ double sh[32];
+    const int r = blockIdx.x;
+    double acc = 0.0;
+    for (int e = ptr[r] + threadIdx.x; e < ptr[r + 1]; e += blockDim.x) {
+        const int row = rows[e];
+        acc += (double)b[row] * (bscale ? (double)bscale[row] : 1.0);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) s[r] = v;
+    }
+}
+
+// y = K^+ s (one CTA)
+__global__ void qk_region_solve(int K, const double* __restrict__ Kp, const double* __restrict__ s,
+                                double* __restrict__ y) {
+    for (int r = threadIdx.x; r < K; r += blockDim.x) {
+        double acc = 0.0;
+        for (int c = 0; c < K; c++) acc += Kp[(long long)r * K + c] * s[c];
+        y[r] = acc;
+    }
+}
+
+// z[row] += y[region of row]
+template <typename T>
+__global__ void qk_region_scatter(int total, const int* __restrict__ rows, const int* __restrict__ rid,
+                                  const double* __restrict__ y, T* __restrict__ z) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < total) z[rows[e]] += (T)y[rid[e]];
+}
+
+}  // namespace
+
+QmsRegions::~QmsRegions() { release(); }
+
+void QmsRegions::release() {
+    void* ps[] = {ptr, rows, rid, Kp, s, y};
+    for (void* p : ps) if (p) cudaFree(p);
+    ptr = rows = rid = nullptr;
+    Kp = s = y = nullptr;
+    K = 0;
+}
+
+int QmsRegions::build(const QGrid& g, const uint8_t* slots, const double* rows6, int nmat, double vshift,
+                      double cut, cudaStream_t st) {
+    release();
+    const int xs = g.xs, ys = g.ys, zs = g.zs, Nx = g.Nx, Ny = g.Ny, Nz = g.Nz;
+    const long long ncell = (long long)xs * ys * zs;
+    // per-slot conductivity per axis and its maximum (slot 0: vacuum)
+    std::vector<double> sax(3 * (nmat + 1), 0.0), smax(nmat + 1, 0.0);
+    for (int r = 0; r < nmat; r++)
+        for (int a = 0; a < 3; a++) {
+            sax[3 * (r + 1) + a] = rows6[r * 6 + 3 + a];
+            smax[r + 1] = std::max(smax[r + 1], rows6[r * 6 + 3 + a]);
+        }
+    auto cid = [&](int i, int j, int k) { return (long long)(i - 1) + (long long)(j - 1) * xs + (long long)(k - 1) * xs * ys; };
+    auto is_cond = [&](long long c) { return smax[slots[c]] > 1.0; };
+    // connected bodies: union-find over conductor cells of one slot (6-neighbours)
+    std::vector<int> par(ncell, -1);                 // ncell < 2^31 (checked at creation)
+    auto find = [&](long long a) -> long long {
+        while (par[a] != a) { par[a] = par[par[a]]; a = par[a]; }
+        return a;
+    };
+    for (int k = 1; k <= zs; k++)
+        for (int j = 1; j <= ys; j++)
+            for (int i = 1; i <= xs; i++) {
+                const long long c = cid(i, j, k);
+                if (!is_cond(c)) continue;
+                par[c] = (int)c;
+                const long long nb[3] = {i > 1 ? cid(i - 1, j, k) : -1, j > 1 ? cid(i, j - 1, k) : -1,
+                                         k > 1 ? cid(i, j, k - 1) : -1};
+                for (long long q : nb)
+                    if (q >= 0 && par[q] >= 0 && slots[q] == slots[c]) {
+                        const long long ra = find(c), rb = find(q);
+                        if (ra != rb) par[std::max(ra, rb)] = (int)std::min(ra, rb);
+                    }
+            }
+    // region of each active V node: body of its incident conductor cell with the largest sigma
+    const long long Nn = g.Nn;
+    std::vector<int> nreg(Nn, -1);
+    std::vector<long long> roots;                   // region index -> body root
+    std::vector<long long> count;
+    std::map<long long, int> rmap;
+    for (int k = 1; k <= Nz; k++)
+        for (int j = 1; j <= Ny; j++)
+            for (int i = 1; i <= Nx; i++) {
+                if (qFixV(g, i, j, k)) continue;
+                double best = -1.0;
+                long long broot = -1;
+                for (int ck = k - 1; ck <= k; ck++)
+                    for (int cj = j - 1; cj <= j; cj++)
+                        for (int ci = i - 1; ci <= i; ci++) {
+                            if (ci < 1 || cj < 1 || ck < 1 || ci > xs || cj > ys || ck > zs) continue;
+                            const long long c = cid(ci, cj, ck);
+                            if (!is_cond(c)) continue;
+                            const long long rt = find(c);
+                            const double sv = smax[slots[c]];
+                            if (sv > best || (sv == best && rt < broot)) { best = sv; broot = rt; }
+                        }
+                if (broot < 0) continue;
+                auto it = rmap.find(broot);
+                int r;
+                if (it == rmap.end()) {
+                    r = (int)roots.size();
+                    rmap[broot] = r;
+                    roots.push_back(broot);
+                    count.push_back(0);
+                } else {
+                    r = it->second;
+                }
+                count[r]++;
+                nreg[(i - 1) + (long long)(j - 1) * Nx + (long long)(k - 1) * Nx * Ny] = r;
+            }
+    int nr = (int)roots.size();
+    if (nr == 0) return 0;
+    // keep at most QMS_REGION_MAX regions (the largest; ties by first appearance)
+    std::vector<int> order(nr), newid(nr, -1);
+    for (int r = 0; r < nr; r++) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return count[a] > count[b]; });
+    const int Kr = std::min(nr, QMS_REGION_MAX);
+    std::vector<int> keep(order.begin(), order.begin() + Kr);
+    std::sort(keep.begin(), keep.end());
+    for (int q = 0; q < Kr; q++) newid[keep[q]] = q;
+    for (long long p = 0; p < Nn; p++)
+        if (nreg[p] >= 0) nreg[p] = newid[nreg[p]];
+    // Galerkin matrix W^T A_V W from the links crossing region boundaries (no cancellation):
+    // link weight max(sigma_edge, floor) / h^2, sigma_edge the mean of the four cells around it
+    const double floor_s = (double)1.0e-12f;
+    const double ih2[3] = {1.0 / (g.dx * g.dx), 1.0 / (g.dy * g.dy), 1.0 / (g.dz * g.dz)};
+    std::vector<double> Km((size_t)Kr * Kr, 0.0);
+    std::vector<double> Tr(Kr, 0.0);              // sum of the V-operator diagonal over each region
+    auto sig_edge = [&](int a, int i, int j, int k) {
+        // edge from node (i,j,k) along axis a: cells with that axis index i/j/k and the other two
+        // indices in {n-1, n}
+        double acc = 0.0;
+        for (int u = 0; u < 2; u++)
+            for (int v = 0; v < 2; v++) {
+                int ci = i, cj = j, ck = k;
+                if (a == 0) { cj = j - 1 + u; ck = k - 1 + v; }
+                else if (a == 1) { ci = i - 1 + u; ck = k - 1 + v; }
+                else { ci = i - 1 + u; cj = j - 1 + v; }
+                if (ci < 1 || cj < 1 || ck < 1 || ci > xs || cj > ys || ck > zs) continue;
+                acc += sax[3 * slots[cid(ci, cj, ck)] + a];
+            }
+        return 0.25 * acc;
+    };
+    for (int k = 1; k <= Nz; k++)
+        for (int j = 1; j <= Ny; j++)
+            for (int i = 1; i <= Nx; i++) {
+                const long long p = (i - 1) + (long long)(j - 1) * Nx + (long long)(k - 1) * Nx * Ny;
+                for (int a = 0; a < 3; a++) {
+                    const int i2 = i + (a == 0), j2 = j + (a == 1), k2 = k + (a == 2);
+                    if (i2 > Nx || j2 > Ny || k2 > Nz) continue;
+                    const long long q = (i2 - 1) + (long long)(j2 - 1) * Nx + (long long)(k2 - 1) * Nx * Ny;
+                    const int R = nreg[p], S = nreg[q];
+                    if (R < 0 && S < 0) continue;
+                    const double w = std::max(sig_edge(a, i, j, k), floor_s) * ih2[a];
+                    if (R >= 0) Tr[R] += (1.0 + vshift) * w;
+                    if (S >= 0) Tr[S] += (1.0 + vshift) * w;
+                    if (vshift != 0.0) {
+                        if (R >= 0) Km[(size_t)R * Kr + R] += vshift * w;
+                        if (S >= 0) Km[(size_t)S * Kr + S] += vshift * w;
+                    }
+                    if (R == S) continue;
+                    if (R >= 0) Km[(size_t)R * Kr + R] += w;
+                    if (S >= 0) Km[(size_t)S * Kr + S] += w;
+                    if (R >= 0 && S >= 0) {
+                        Km[(size_t)R * Kr + S] -= w;
+                        Km[(size_t)S * Kr + R] -= w;
+                    }
+                }
+            }
+    // pseudo-inverse, scaled by each region's own stiffness T_R (the sum of the V-operator
+    // diagonal over its nodes), so that its eigenvalues compare with those of the row-scaled
+    // fine operator: the constant of an isolated conductor (coupled only through the floor)
+    // lands near 1e-19 and is dropped, a body attached to others through a few edges keeps
+    // its small but resolvable eigenvalue.  `cut` bounds the amplification 1/lambda to what
+    // the inner vectors' precision carries.
+    std::vector<double> dsq(Kr), A((size_t)Kr * Kr), Q;
+    for (int r = 0; r < Kr; r++) dsq[r] = Tr[r] > 0 ? 1.0 / std::sqrt(Tr[r]) : 0.0;
+    for (int r = 0; r < Kr; r++)
+        for (int c = 0; c < Kr; c++) A[(size_t)r * Kr + c] = Km[(size_t)r * Kr + c] * dsq[r] * dsq[c];
+    sym_eig_jacobi(Kr, A, Q);
+    std::vector<double> Kpi((size_t)Kr * Kr, 0.0);
+    int kept = 0;
+    for (int e = 0; e < Kr; e++) {
+        const double lam = A[(size_t)e * Kr + e];
+        if (!(lam > cut)) continue;
+        kept++;
+        for (int r = 0; r < Kr; r++)
+            for (int c = 0; c < Kr; c++)
+                Kpi[(size_t)r * Kr + c] += Q[(size_t)r * Kr + e] * Q[(size_t)c * Kr + e] / lam;
+    }
+    if (kept == 0) return 0;                          // only null modes: nothing to add
+    for (int r = 0; r < Kr; r++)
+        for (int c = 0; c < Kr; c++) Kpi[(size_t)r * Kr + c] *= dsq[r] * dsq[c];
+    // node lists, region by region
+    std::vector<int> hptr(Kr + 1, 0), hrows, hrid;
+    for (long long p = 0; p < Nn; p++)
+        if (nreg[p] >= 0) hptr[nreg[p] + 1]++;
+    for (int r = 0; r < Kr; r++) hptr[r + 1] += hptr[r];
+    hrows.resize(hptr[Kr]);
+    hrid.resize(hptr[Kr]);
+    std::vector<int> fill(hptr.begin(), hptr.end() - 1);
+    for (long long p = 0; p < Nn; p++)
+        if (nreg[p] >= 0) {
+            const int r = nreg[p];
+            hrows[fill[r]] = (int)(g.oV + p);
+            hrid[fill[r]] = r;
+            fill[r]++;
+        }
+    const int total = hptr[Kr];
+    if (cudaMalloc(&ptr, (Kr + 1) * sizeof(int)) != cudaSuccess || cudaMalloc(&rows, total * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&rid, total * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&Kp, (size_t)Kr * Kr * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&s, Kr * sizeof(double)) != cudaSuccess || cudaMalloc(&y, Kr * sizeof(double)) != cudaSuccess) {
+        err = "out of device memory (region coarse space)";
+        release();
+        return -1;
+    }
+    cudaMemcpyAsync(ptr, hptr.data(), (Kr + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(rows, hrows.data(), total * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(rid, hrid.data(), total * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(Kp, Kpi.data(), (size_t)Kr * Kr * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) {   // the host vectors go out of scope
+        err = "region coarse space upload failed";
+        release();
+        return -1;
+    }
+    K = Kr;
+    total_entries = total;
+    return 0;
+}
+
+template <typename T>
+void QmsRegions::apply(const T* b, const float* bscale, T* z, cudaStream_t st, long long& launches) {
+    if (K == 0) return;
+    qk_region_sums<T><<<K, 256, 0, st>>>(ptr, rows, b, bscale, s);
+    qk_region_solve<<<1, 256, 0, st>>>(K, Kp, s, y);
+    const int total = total_entries;
+    qk_region_scatter<T><<<(total + 255) / 256, 256, 0, st>>>(total, rows, rid, y, z);
+    launches += 3;
+}
+template void QmsRegions::apply<float>(const float*, const float*, float*, cudaStream_t, long long&);
+template void QmsRegions::apply<double>(const double*, const float*, double*, cudaStream_t, long long&);

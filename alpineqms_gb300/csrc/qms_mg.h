@@ -56,3 +56,33 @@ struct QmsMG {
     int build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T vshift, cudaStream_t st);
     int vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v, cudaStream_t st);
 };
+
+// Coarse space of the V block spanned by one indicator vector per conductor region (a
+// connected body of cells of one material with sigma > 1 S/m; a V node belongs to the
+// region of its incident conductor cell with the largest sigma).  Potential offsets of
+// bodies that touch others only through a few edges are near-null modes of the V
+// operator that the geometric aggregation cannot represent; this space captures them.
+// Applied additively to the multigrid V-cycle: z_V += W K^+ W^T (bscale .* r)_V, with K
+// the Galerkin matrix W^T A_V W and K^+ its pseudo-inverse (the constant of every
+// isolated conductor is a null mode and is dropped).
+#define QMS_REGION_MAX 1024
+struct QmsRegions {
+    int K = 0;                    // regions carrying a coarse degree of freedom (0: disabled)
+    int total_entries = 0;        // V rows in all regions
+    int* ptr = nullptr;           // K+1 offsets into rows
+    int* rows = nullptr;          // V rows (global unknown index) of each region, region by region
+    int* rid = nullptr;           // region of each entry of rows
+    double* Kp = nullptr;         // K x K pseudo-inverse, row-major
+    double* s = nullptr;          // K region sums / coarse solution
+    double* y = nullptr;
+    std::string err;
+    ~QmsRegions();
+    void release();
+    // slots: xs*ys*zs host material slots; rows6: per-slot mu_r xyz, sigma xyz (slot s at s-1)
+    int build(const QGrid& g, const uint8_t* slots, const double* rows6, int nmat, double vshift, double cut,
+              cudaStream_t st);
+    // z_V += W K^+ W^T (bscale .* b)_V  (bscale may be null)
+    template <typename T>
+    void apply(const T* b, const float* bscale, T* z, cudaStream_t st, long long& launches);
+};
+

@@ -45,7 +45,7 @@ __device__ __forceinline__ T op_div(T a, T d) {
 }
 
 template <typename T, bool ADV, int MODE>
-__global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const T* __restrict__ b,
               T* __restrict__ y, const T* __restrict__ w, double* __restrict__ partials) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -122,21 +122,21 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T mx_im = CF(0, cur, 0, -1), mx_i = CF(0, cur, 0, 0);
                     const T svy = ADV ? s * P.vy : T(0), svz = ADV ? s * P.vz : T(0);
                     const T d = (mz_j + mz_jm) * P.idy2 + (my_k + my_km) * P.idz2 + (mx_i + mx_im) * P.idx2 + s * P.idt;
-                    T acc = d * XS(0, x0, 0, 0);
-                    acc += (-my_km * P.idz2 + svz * P.i2dz) * XS(0, xm, 0, 0);
-                    acc += (-mz_jm * P.idy2 + svy * P.i2dy) * XS(0, x0, -1, 0);
-                    acc += (-mx_im * P.idx2) * XS(0, x0, 0, -1);
-                    acc += (-mx_i * P.idx2) * XS(0, x0, 0, 1);
-                    acc += (-mz_j * P.idy2 - svy * P.i2dy) * XS(0, x0, 1, 0);
-                    acc += (-my_k * P.idz2 - svz * P.i2dz) * XS(0, xp, 0, 0);
-                    acc += (mz_jm * P.idxdy - svy * P.i2dx) * XS(1, x0, -1, 0);
-                    acc += (-mz_jm * P.idxdy + svy * P.i2dx) * XS(1, x0, -1, 1);
-                    acc += (-mz_j * P.idxdy - svy * P.i2dx) * XS(1, x0, 0, 0);
-                    acc += (mz_j * P.idxdy + svy * P.i2dx) * XS(1, x0, 0, 1);
-                    acc += (my_km * P.idxdz - svz * P.i2dx) * XS(2, xm, 0, 0);
-                    acc += (-my_km * P.idxdz + svz * P.i2dx) * XS(2, xm, 0, 1);
-                    acc += (-my_k * P.idxdz - svz * P.i2dx) * XS(2, x0, 0, 0);
-                    acc += (my_k * P.idxdz + svz * P.i2dx) * XS(2, x0, 0, 1);
+                    // difference form: every coupling pair is applied to a difference of unknowns,
+                    // so the rounding error scales with the variation of x, not with x itself
+                    const T X0 = XS(0, x0, 0, 0);
+                    T acc = s * P.idt * X0;
+                    acc += my_km * P.idz2 * (X0 - XS(0, xm, 0, 0)) + my_k * P.idz2 * (X0 - XS(0, xp, 0, 0));
+                    acc += mz_jm * P.idy2 * (X0 - XS(0, x0, -1, 0)) + mz_j * P.idy2 * (X0 - XS(0, x0, 1, 0));
+                    acc += mx_im * P.idx2 * (X0 - XS(0, x0, 0, -1)) + mx_i * P.idx2 * (X0 - XS(0, x0, 0, 1));
+                    if (ADV) {
+                        acc += svz * P.i2dz * (XS(0, xm, 0, 0) - XS(0, xp, 0, 0));
+                        acc += svy * P.i2dy * (XS(0, x0, -1, 0) - XS(0, x0, 1, 0));
+                    }
+                    acc += (mz_jm * P.idxdy - svy * P.i2dx) * (XS(1, x0, -1, 0) - XS(1, x0, -1, 1));
+                    acc += (mz_j * P.idxdy + svy * P.i2dx) * (XS(1, x0, 0, 1) - XS(1, x0, 0, 0));
+                    acc += (my_km * P.idxdz - svz * P.i2dx) * (XS(2, xm, 0, 0) - XS(2, xm, 0, 1));
+                    acc += (my_k * P.idxdz + svz * P.i2dx) * (XS(2, x0, 0, 1) - XS(2, x0, 0, 0));
                     acc += s * P.idx * (XS(3, x0, 0, 1) - XS(3, x0, 0, 0));
                     emit(row, acc, d, true);
                 }
@@ -154,21 +154,19 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T my_jm = CF(1, cur, -1, 0), my_j = CF(1, cur, 0, 0);
                     const T svx = ADV ? s * P.vx : T(0), svz = ADV ? s * P.vz : T(0);
                     const T d = (mz_i + mz_im) * P.idx2 + (mx_k + mx_km) * P.idz2 + (my_j + my_jm) * P.idy2 + s * P.idt;
-                    T acc = d * XS(1, x0, 0, 0);
-                    acc += (mz_im * P.idxdy - svx * P.i2dy) * XS(0, x0, 0, -1);
-                    acc += (-mz_i * P.idxdy - svx * P.i2dy) * XS(0, x0, 0, 0);
-                    acc += (-mz_im * P.idxdy + svx * P.i2dy) * XS(0, x0, 1, -1);
-                    acc += (mz_i * P.idxdy + svx * P.i2dy) * XS(0, x0, 1, 0);
-                    acc += (-mx_km * P.idz2 + svz * P.i2dz) * XS(1, xm, 0, 0);
-                    acc += (-my_jm * P.idy2) * XS(1, x0, -1, 0);
-                    acc += (-mz_im * P.idx2 + svx * P.i2dx) * XS(1, x0, 0, -1);
-                    acc += (-mz_i * P.idx2 - svx * P.i2dx) * XS(1, x0, 0, 1);
-                    acc += (-my_j * P.idy2) * XS(1, x0, 1, 0);
-                    acc += (-mx_k * P.idz2 - svz * P.i2dz) * XS(1, xp, 0, 0);
-                    acc += (mx_km * P.idydz - svz * P.i2dy) * XS(2, xm, 0, 0);
-                    acc += (-mx_km * P.idydz + svz * P.i2dy) * XS(2, xm, 1, 0);
-                    acc += (-mx_k * P.idydz - svz * P.i2dy) * XS(2, x0, 0, 0);
-                    acc += (mx_k * P.idydz + svz * P.i2dy) * XS(2, x0, 1, 0);
+                    const T Y0 = XS(1, x0, 0, 0);
+                    T acc = s * P.idt * Y0;
+                    acc += mx_km * P.idz2 * (Y0 - XS(1, xm, 0, 0)) + mx_k * P.idz2 * (Y0 - XS(1, xp, 0, 0));
+                    acc += my_jm * P.idy2 * (Y0 - XS(1, x0, -1, 0)) + my_j * P.idy2 * (Y0 - XS(1, x0, 1, 0));
+                    acc += mz_im * P.idx2 * (Y0 - XS(1, x0, 0, -1)) + mz_i * P.idx2 * (Y0 - XS(1, x0, 0, 1));
+                    if (ADV) {
+                        acc += svz * P.i2dz * (XS(1, xm, 0, 0) - XS(1, xp, 0, 0));
+                        acc += svx * P.i2dx * (XS(1, x0, 0, -1) - XS(1, x0, 0, 1));
+                    }
+                    acc += (mz_im * P.idxdy - svx * P.i2dy) * (XS(0, x0, 0, -1) - XS(0, x0, 1, -1));
+                    acc += (mz_i * P.idxdy + svx * P.i2dy) * (XS(0, x0, 1, 0) - XS(0, x0, 0, 0));
+                    acc += (mx_km * P.idydz - svz * P.i2dy) * (XS(2, xm, 0, 0) - XS(2, xm, 1, 0));
+                    acc += (mx_k * P.idydz + svz * P.i2dy) * (XS(2, x0, 1, 0) - XS(2, x0, 0, 0));
                     acc += s * P.idy * (XS(3, x0, 1, 0) - XS(3, x0, 0, 0));
                     emit(row, acc, d, true);
                 }
@@ -186,21 +184,19 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T mz_km = CF(2, prv, 0, 0), mz_k = CF(2, cur, 0, 0);
                     const T svx = ADV ? s * P.vx : T(0), svy = ADV ? s * P.vy : T(0);
                     const T d = (my_i + my_im) * P.idx2 + (mx_j + mx_jm) * P.idy2 + (mz_k + mz_km) * P.idz2 + s * P.idt;
-                    T acc = d * XS(2, x0, 0, 0);
-                    acc += (my_im * P.idxdz - svx * P.i2dz) * XS(0, x0, 0, -1);
-                    acc += (-my_i * P.idxdz - svx * P.i2dz) * XS(0, x0, 0, 0);
-                    acc += (-my_im * P.idxdz + svx * P.i2dz) * XS(0, xp, 0, -1);
-                    acc += (my_i * P.idxdz + svx * P.i2dz) * XS(0, xp, 0, 0);
-                    acc += (mx_jm * P.idydz - svy * P.i2dz) * XS(1, x0, -1, 0);
-                    acc += (-mx_j * P.idydz - svy * P.i2dz) * XS(1, x0, 0, 0);
-                    acc += (-mx_jm * P.idydz + svy * P.i2dz) * XS(1, xp, -1, 0);
-                    acc += (mx_j * P.idydz + svy * P.i2dz) * XS(1, xp, 0, 0);
-                    acc += (-mz_km * P.idz2) * XS(2, xm, 0, 0);
-                    acc += (-mx_jm * P.idy2 + svy * P.i2dy) * XS(2, x0, -1, 0);
-                    acc += (-my_im * P.idx2 + svx * P.i2dx) * XS(2, x0, 0, -1);
-                    acc += (-my_i * P.idx2 - svx * P.i2dx) * XS(2, x0, 0, 1);
-                    acc += (-mx_j * P.idy2 - svy * P.i2dy) * XS(2, x0, 1, 0);
-                    acc += (-mz_k * P.idz2) * XS(2, xp, 0, 0);
+                    const T Z0 = XS(2, x0, 0, 0);
+                    T acc = s * P.idt * Z0;
+                    acc += mz_km * P.idz2 * (Z0 - XS(2, xm, 0, 0)) + mz_k * P.idz2 * (Z0 - XS(2, xp, 0, 0));
+                    acc += mx_jm * P.idy2 * (Z0 - XS(2, x0, -1, 0)) + mx_j * P.idy2 * (Z0 - XS(2, x0, 1, 0));
+                    acc += my_im * P.idx2 * (Z0 - XS(2, x0, 0, -1)) + my_i * P.idx2 * (Z0 - XS(2, x0, 0, 1));
+                    if (ADV) {
+                        acc += svy * P.i2dy * (XS(2, x0, -1, 0) - XS(2, x0, 1, 0));
+                        acc += svx * P.i2dx * (XS(2, x0, 0, -1) - XS(2, x0, 0, 1));
+                    }
+                    acc += (my_im * P.idxdz - svx * P.i2dz) * (XS(0, x0, 0, -1) - XS(0, xp, 0, -1));
+                    acc += (my_i * P.idxdz + svx * P.i2dz) * (XS(0, xp, 0, 0) - XS(0, x0, 0, 0));
+                    acc += (mx_jm * P.idydz - svy * P.i2dz) * (XS(1, x0, -1, 0) - XS(1, xp, -1, 0));
+                    acc += (mx_j * P.idydz + svy * P.i2dz) * (XS(1, xp, 0, 0) - XS(1, x0, 0, 0));
                     acc += s * P.idz * (XS(3, xp, 0, 0) - XS(3, x0, 0, 0));
                     emit(row, acc, d, true);
                 }
@@ -219,49 +215,50 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                     const T fy0 = fmax(sy0, P.sigfloor), fy1 = fmax(sy1, P.sigfloor);
                     const T fz0 = fmax(sz0, P.sigfloor), fz1 = fmax(sz1, P.sigfloor);
                     const T d = (fx0 + fx1) * P.idx2 + (fy0 + fy1) * P.idy2 + (fz0 + fz1) * P.idz2;
-                    T acc = d * XS(3, x0, 0, 0);
-                    acc -= fz1 * P.idz2 * XS(3, xm, 0, 0);
-                    acc -= fy1 * P.idy2 * XS(3, x0, -1, 0);
-                    acc -= fx1 * P.idx2 * XS(3, x0, 0, -1);
-                    acc -= fx0 * P.idx2 * XS(3, x0, 0, 1);
-                    acc -= fy0 * P.idy2 * XS(3, x0, 1, 0);
-                    acc -= fz0 * P.idz2 * XS(3, xp, 0, 0);
+                    const T V0 = XS(3, x0, 0, 0);
+                    T acc = fz1 * P.idz2 * (V0 - XS(3, xm, 0, 0)) + fz0 * P.idz2 * (V0 - XS(3, xp, 0, 0));
+                    acc += fy1 * P.idy2 * (V0 - XS(3, x0, -1, 0)) + fy0 * P.idy2 * (V0 - XS(3, x0, 1, 0));
+                    acc += fx1 * P.idx2 * (V0 - XS(3, x0, 0, -1)) + fx0 * P.idx2 * (V0 - XS(3, x0, 0, 1));
                     const T axm = XS(0, x0, 0, -1), ax0 = XS(0, x0, 0, 0);
                     const T aym = XS(1, x0, -1, 0), ay0 = XS(1, x0, 0, 0);
                     const T azm = XS(2, xm, 0, 0), az0 = XS(2, x0, 0, 0);
-                    acc += P.idt * ((sx0 * ax0 - sx1 * axm) * P.idx + (sy0 * ay0 - sy1 * aym) * P.idy +
-                                    (sz0 * az0 - sz1 * azm) * P.idz);
+                    // div(sigma A) / dt: s0 a0 - s1 a1 = s0 (a0 - a1) + (s0 - s1) a1 (exact inside a body)
+                    acc += P.idt * ((sx0 * (ax0 - axm) + (sx0 - sx1) * axm) * P.idx +
+                                    (sy0 * (ay0 - aym) + (sy0 - sy1) * aym) * P.idy +
+                                    (sz0 * (az0 - azm) + (sz0 - sz1) * azm) * P.idz);
                     if (ADV) {
+                        // div(sigma v x curl A), grouped by velocity component into differences
                         const T vx = P.vx, vy = P.vy, vz = P.vz;
-                        acc += (sx1 * vz * P.i2dxdz - sz1 * vx * P.i2dz2) * XS(0, xm, 0, -1);
-                        acc += (-sx0 * vz * P.i2dxdz - sz1 * vx * P.i2dz2) * XS(0, xm, 0, 0);
-                        acc += (sx1 * vy * P.i2dxdy - sy1 * vx * P.i2dy2) * XS(0, x0, -1, -1);
-                        acc += (-sx0 * vy * P.i2dxdy - sy1 * vx * P.i2dy2) * XS(0, x0, -1, 0);
-                        acc += ((sy0 + sy1) * vx * P.i2dy2 + (sz0 + sz1) * vx * P.i2dz2) * (axm + ax0);
-                        acc += (-sx1 * vy * P.i2dxdy - sy0 * vx * P.i2dy2) * XS(0, x0, 1, -1);
-                        acc += (sx0 * vy * P.i2dxdy - sy0 * vx * P.i2dy2) * XS(0, x0, 1, 0);
-                        acc += (-sx1 * vz * P.i2dxdz - sz0 * vx * P.i2dz2) * XS(0, xp, 0, -1);
-                        acc += (sx0 * vz * P.i2dxdz - sz0 * vx * P.i2dz2) * XS(0, xp, 0, 0);
-
-                        acc += (sy1 * vz * P.i2dydz - sz1 * vy * P.i2dz2) * XS(1, xm, -1, 0);
-                        acc += (-sy0 * vz * P.i2dydz - sz1 * vy * P.i2dz2) * XS(1, xm, 0, 0);
-                        acc += (-sx1 * vy * P.i2dx2 + sy1 * vx * P.i2dxdy) * XS(1, x0, -1, -1);
-                        acc += ((sx0 + sx1) * vy * P.i2dx2 + (sz0 + sz1) * vy * P.i2dz2) * (aym + ay0);
-                        acc += (-sx0 * vy * P.i2dx2 - sy1 * vx * P.i2dxdy) * XS(1, x0, -1, 1);
-                        acc += (-sx1 * vy * P.i2dx2 - sy0 * vx * P.i2dxdy) * XS(1, x0, 0, -1);
-                        acc += (-sx0 * vy * P.i2dx2 + sy0 * vx * P.i2dxdy) * XS(1, x0, 0, 1);
-                        acc += (-sy1 * vz * P.i2dydz - sz0 * vy * P.i2dz2) * XS(1, xp, -1, 0);
-                        acc += (sy0 * vz * P.i2dydz - sz0 * vy * P.i2dz2) * XS(1, xp, 0, 0);
-
-                        acc += (-sy1 * vz * P.i2dy2 + sz1 * vy * P.i2dydz) * XS(2, xm, -1, 0);
-                        acc += (-sx1 * vz * P.i2dx2 + sz1 * vx * P.i2dxdz) * XS(2, xm, 0, -1);
-                        acc += ((sx0 + sx1) * vz * P.i2dx2 + (sy0 + sy1) * vz * P.i2dy2) * (azm + az0);
-                        acc += (-sx0 * vz * P.i2dx2 - sz1 * vx * P.i2dxdz) * XS(2, xm, 0, 1);
-                        acc += (-sy0 * vz * P.i2dy2 - sz1 * vy * P.i2dydz) * XS(2, xm, 1, 0);
-                        acc += (-sy1 * vz * P.i2dy2 - sz0 * vy * P.i2dydz) * XS(2, x0, -1, 0);
-                        acc += (-sx1 * vz * P.i2dx2 - sz0 * vx * P.i2dxdz) * XS(2, x0, 0, -1);
-                        acc += (-sx0 * vz * P.i2dx2 + sz0 * vx * P.i2dxdz) * XS(2, x0, 0, 1);
-                        acc += (-sy0 * vz * P.i2dy2 + sz0 * vy * P.i2dydz) * XS(2, x0, 1, 0);
+                        // Ax neighbours
+                        const T SA = axm + ax0;
+                        acc += vz * P.i2dxdz * (sx1 * (XS(0, xm, 0, -1) - XS(0, xp, 0, -1)) +
+                                                 sx0 * (XS(0, xp, 0, 0) - XS(0, xm, 0, 0)));
+                        acc += vy * P.i2dxdy * (sx1 * (XS(0, x0, -1, -1) - XS(0, x0, 1, -1)) +
+                                                 sx0 * (XS(0, x0, 1, 0) - XS(0, x0, -1, 0)));
+                        acc += vx * P.i2dy2 * (sy1 * (SA - (XS(0, x0, -1, -1) + XS(0, x0, -1, 0))) +
+                                               sy0 * (SA - (XS(0, x0, 1, -1) + XS(0, x0, 1, 0))));
+                        acc += vx * P.i2dz2 * (sz1 * (SA - (XS(0, xm, 0, -1) + XS(0, xm, 0, 0))) +
+                                               sz0 * (SA - (XS(0, xp, 0, -1) + XS(0, xp, 0, 0))));
+                        // Ay neighbours
+                        const T SB = aym + ay0;
+                        acc += vz * P.i2dydz * (sy1 * (XS(1, xm, -1, 0) - XS(1, xp, -1, 0)) +
+                                                 sy0 * (XS(1, xp, 0, 0) - XS(1, xm, 0, 0)));
+                        acc += vx * P.i2dxdy * (sy1 * (XS(1, x0, -1, -1) - XS(1, x0, -1, 1)) +
+                                                 sy0 * (XS(1, x0, 0, 1) - XS(1, x0, 0, -1)));
+                        acc += vy * P.i2dx2 * (sx1 * (SB - (XS(1, x0, -1, -1) + XS(1, x0, 0, -1))) +
+                                               sx0 * (SB - (XS(1, x0, -1, 1) + XS(1, x0, 0, 1))));
+                        acc += vy * P.i2dz2 * (sz1 * (SB - (XS(1, xm, -1, 0) + XS(1, xm, 0, 0))) +
+                                               sz0 * (SB - (XS(1, xp, -1, 0) + XS(1, xp, 0, 0))));
+                        // Az neighbours
+                        const T SC = azm + az0;
+                        acc += vy * P.i2dydz * (sz1 * (XS(2, xm, -1, 0) - XS(2, xm, 1, 0)) +
+                                                 sz0 * (XS(2, x0, 1, 0) - XS(2, x0, -1, 0)));
+                        acc += vx * P.i2dxdz * (sz1 * (XS(2, xm, 0, -1) - XS(2, xm, 0, 1)) +
+                                                 sz0 * (XS(2, x0, 0, 1) - XS(2, x0, 0, -1)));
+                        acc += vz * P.i2dx2 * (sx1 * (SC - (XS(2, xm, 0, -1) + XS(2, x0, 0, -1))) +
+                                               sx0 * (SC - (XS(2, xm, 0, 1) + XS(2, x0, 0, 1))));
+                        acc += vz * P.i2dy2 * (sy1 * (SC - (XS(2, xm, -1, 0) + XS(2, x0, -1, 0))) +
+                                               sy0 * (SC - (XS(2, xm, 1, 0) + XS(2, x0, 1, 0))));
                     }
                     emit(row, acc, d, false);
                 }

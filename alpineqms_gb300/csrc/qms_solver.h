@@ -19,6 +19,7 @@ struct QmsSolver {
     cudaStream_t st = nullptr;
     bool own_stream = false;
     bool fp64_inner = false;
+    bool trace = false;         // QMS_TRACE set: one stderr line per refinement iteration
     size_t tsize = 4;
     long long vec_blocks = 0, nbop = 0;
 
@@ -30,6 +31,7 @@ struct QmsSolver {
     double* x = nullptr;        // current solution [Ax|Ay|Az|V]
     double* b = nullptr;        // RHS of the last solve
     double* r64 = nullptr;      // scaled FP64 residual
+    double* xbest = nullptr;    // best iterate of the current solve
     double* H = nullptr;        // Hx|Hy|Hz cubes
     double* slicebuf = nullptr;
     double* part = nullptr;     // block partial sums
@@ -45,6 +47,7 @@ struct QmsSolver {
     QmsMG<float> mgf[2];        // hierarchies of the steady [0] and transient [1] operators (mixed)
     QmsMG<double> mgd[2];       // the same in FP64 (plain FP64 solver)
     bool use_mg = false;
+    QmsRegions regions;         // conductor-region coarse space of the V block (with MG)
     // z = preconditioner(r): multigrid on (bscale .* r) or the Jacobi / identity fallback
     template <typename T> void precond(const T* r, const float* bscale, T* z, bool mask_v, bool transient,
                                        bool jacobi_pcg);
@@ -98,7 +101,6 @@ struct QmsSolver {
     bool graph_resid_ready = false;
     int gm_k_est = 0;           // FGMRES iterations replayed per refinement iteration (0: not yet known)
     int gm_k_seen = 0;          // largest count seen while running with host checks
-    template <typename T> void revert_last(double nrm);
     void* gmV[33] = {};         // FGMRES basis (m + 1) and preconditioned directions (m)
     void* gmZ[32] = {};
     double* gm_H = nullptr;     // Hessenberg matrix (m+1) x m, row-major with stride m

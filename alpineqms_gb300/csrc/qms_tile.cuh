@@ -10,6 +10,10 @@
 #define OTX 32
 #define OTY 8
 #define OKB 16
+// resident CTAs per SM the FP32 stencil kernels are compiled for (caps registers at 64)
+#ifndef QMS_STENCIL_MINB
+#define QMS_STENCIL_MINB 4
+#endif
 
 // three-plane ring: planes k-1 and k are read while plane k+1 is filled, so a
 // single barrier per plane separates the fill of one plane from its first use

@@ -209,6 +209,117 @@ class QMSServer:
         return [self._results[k] for k in sorted(self._results)]
 
 
+class NativeServer:
+    """The serving object of libqms_gb300 (``qms_srv_*`` in include/qms.h): the same FIFO
+    admission under an HBM budget and slot limit as QMSServer, with the admission and
+    the per-request solves run by native threads.  Requests and results use the same
+    SolveRequest / SolveResult types; a result's slice records have the layout of
+    Backend.run."""
+
+    def __init__(self, budget_bytes: int = 150 << 30, max_resident: int = 16, device: int = 0,
+                 precision: str = "mixed"):
+        import ctypes
+        from . import _lib
+        self._ct = ctypes
+        self._lib = _lib
+        self.L = _lib.load()
+        self.precision = _lib.QMS_PREC_FP64 if precision == "fp64" else _lib.QMS_PREC_MIXED
+        d = _lib.QmsSrvDesc(float(budget_bytes), int(max_resident), int(device))
+        self.h = ctypes.c_void_p()
+        rc = self.L.qms_srv_create(ctypes.byref(d), ctypes.byref(self.h))
+        if rc:
+            raise _lib.QMSError(rc, f"qms_srv_create: {_lib.ERRORS.get(rc, rc)}")
+        self._reqs: Dict[int, SolveRequest] = {}
+
+    def submit(self, req: SolveRequest) -> int:
+        ct, lib = self._ct, self._lib
+        i = req.inputs
+        r = lib.QmsRequest()
+        r.xs, r.ys, r.zs = i.xs, i.ys, i.zs
+        r.dx, r.dy, r.dz, r.dt = i.dx, i.dy, i.dz, i.dt
+        r.nt, r.tt = i.nt, i.tt
+        r.slice_axis = {"x": 0, "y": 1, "z": 2}[i.slice_axis]
+        r.slice_index = i.slice_index
+        r.keep = lib.QMS_KEEP_SLICES if req.keep_fields == "slice" else lib.QMS_KEEP_NONE
+        r.precision = self.precision
+        for c in range(3):
+            r.B[c] = float(i.B[c])
+        for c, g in enumerate(np.asarray(i.G, dtype=np.float64).reshape(9)):
+            r.G[c] = float(g)
+        for d, t in enumerate(i.traj):
+            r.traj[d][0], r.traj[d][1], r.traj[d][2] = float(t.v0), float(t.accel), float(t.n_accel)
+        if i.excitation is None:
+            r.exc_kind = lib.QMS_EXC_NONE
+        else:
+            kind, f, ph = i.excitation
+            r.exc_kind = lib.QMS_EXC_COS if kind == "cos" else lib.QMS_EXC_SIN
+            r.exc_f, r.exc_phase = float(f), float(ph)
+        geom = np.ascontiguousarray(req.geom, dtype=np.float64)
+        table = np.ascontiguousarray(i.props_table(), dtype=np.float64)
+        r.geom, r.table, r.nmat = geom.ctypes.data, table.ctypes.data, table.shape[0]
+        rid = ct.c_longlong()
+        rc = self.L.qms_srv_submit(self.h, ct.byref(r), ct.byref(rid))   # copies geom and table
+        if rc:
+            raise lib.QMSError(rc, f"qms_srv_submit: {lib.ERRORS.get(rc, rc)}")
+        req.request_id = int(rid.value)
+        self._reqs[req.request_id] = req
+        return req.request_id
+
+    def wait(self, rid: int) -> SolveResult:
+        ct, lib = self._ct, self._lib
+        out = lib.QmsSrvResult()
+        self.L.qms_srv_wait(self.h, rid, ct.byref(out))
+        req = self._reqs[rid]
+        i = req.inputs
+        slices = []
+        if out.n_slice_values > 0:
+            buf = np.empty(out.n_slice_values, np.float64)
+            self.L.qms_srv_slices(self.h, rid, buf.ctypes.data, buf.size)
+            n1, n2 = i.slice_shape()
+            m = n1 * n2
+            for rec in buf.reshape(-1, 3 * m):
+                slices.append(np.concatenate([rec[q * m:(q + 1) * m].reshape((n1, n2), order="F")
+                                              for q in range(3)]).ravel())
+        status = {lib.QMS_SRV_DONE: "ok", lib.QMS_SRV_FAILED: "failed", lib.QMS_SRV_REJECTED: "rejected"}.get(
+            out.state, "unknown")
+        err = self.L.qms_srv_error(self.h, rid)
+        return SolveResult(rid, int(out.n_dims), int(out.steps_done), out.arrival_s, out.admitted_s, out.finished_s,
+                           [out.step_mean_s] * int(out.steps_done), out.steady_s, slices, None, status,
+                           err.decode() if err else "")
+
+    def serve(self, requests: List[SolveRequest], gaps: Optional[List[float]] = None) -> List[SolveResult]:
+        t0 = time.perf_counter()
+        t_next = 0.0
+        ids = []
+        for q, req in enumerate(requests):
+            if gaps is not None:
+                t_next += gaps[q]
+                delay = t_next - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+            ids.append(self.submit(req))
+        return [self.wait(r) for r in ids]
+
+    def stats(self) -> Dict:
+        ct, lib = self._ct, self._lib
+        st = lib.QmsSrvStats()
+        self.L.qms_srv_stats_get(self.h, ct.byref(st))
+        out = {k: getattr(st, k) for k, _ in lib.QmsSrvStats._fields_}
+        out["dof_timesteps_per_s"] = st.dof_timesteps / st.wall_s if st.wall_s > 0 else None
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.qms_srv_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 def latency_report(results: List[SolveResult], wall: float) -> Dict:
     ok = [r for r in results if r.status == "ok"]
     steps = np.array([x for r in ok for x in r.step_latency]) if ok else np.zeros(0)
@@ -256,15 +367,28 @@ def main(argv=None):
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--max-resident", type=int, default=16)
     ap.add_argument("--precision", default="mixed")
+    ap.add_argument("--scheduler", default="native", choices=["native", "python"])
     a = ap.parse_args(argv)
     reqs, gaps = poisson_stream(a.requests, a.mean_gap, nt=a.steps)
-    srv = QMSServer(int(a.budget_gb * (1 << 30)), a.max_resident, Backend(precision=a.precision))
+    budget = int(a.budget_gb * (1 << 30))
     t0 = time.perf_counter()
-    res = srv.serve(reqs, gaps)
-    wall = time.perf_counter() - t0
-    rep = latency_report(res, wall)
-    rep.update({"peak_resident": srv.peak_resident, "peak_bytes": srv.peak_bytes, "mean_gap_s": a.mean_gap,
-                "steps_per_request": a.steps, "precision": a.precision})
+    if a.scheduler == "native":
+        with NativeServer(budget, a.max_resident, precision=a.precision) as srv:
+            res = srv.serve(reqs, gaps)
+            wall = time.perf_counter() - t0
+            rep = latency_report(res, wall)
+            st = srv.stats()
+            # per-step percentiles from the native per-step timings
+            rep.update({"step_p50_ms": st["step_p50_ms"], "step_p99_ms": st["step_p99_ms"],
+                        "peak_resident": st["peak_resident"], "peak_bytes": st["peak_bytes"]})
+    else:
+        srv = QMSServer(budget, a.max_resident, Backend(precision=a.precision))
+        res = srv.serve(reqs, gaps)
+        wall = time.perf_counter() - t0
+        rep = latency_report(res, wall)
+        rep.update({"peak_resident": srv.peak_resident, "peak_bytes": srv.peak_bytes})
+    rep.update({"scheduler": a.scheduler, "mean_gap_s": a.mean_gap, "steps_per_request": a.steps,
+                "precision": a.precision})
     print(json.dumps(rep))
 
 

@@ -92,6 +92,10 @@ typedef struct {
     int gmres_m;             /* FGMRES basis size per refinement iteration (<= 32) */
     int use_graphs;          /* replay each refinement iteration of a step as one CUDA graph, with the
                                 FGMRES iteration count learned from the first solve (1 = on) */
+    double mg_region_cut;    /* conductor-region coarse space of the potential block: eigenvalues of
+                                its region-stiffness-scaled Galerkin matrix at or below this are
+                                dropped (0 = automatic: 1e-9 with FP64 inner vectors, 1e-6 with FP32;
+                                negative = no region space) */
 } qms_desc;
 
 typedef struct {
@@ -193,6 +197,86 @@ void* qms_get_stream(qms_handle* h);
 int qms_residual_noalloc(int xs, int ys, int zs, double dx, double dy, double dz, double dt, int transient,
                          const double v[3], const uint8_t* d_slots, const double* rows, int nmat,
                          const double* d_x, const double* d_b, double* d_r, double* d_sums, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Serving: whole solves (the content of one inputs.txt + geom.bin pair, as
+ * the reference program reads them, 3D/master.py:16-77) submitted to a
+ * server object that admits them in arrival order while an HBM budget and a
+ * slot limit allow, charging each its qms_device_bytes footprint.  Every
+ * admitted solve is resident on its own handle, CUDA stream and worker thread,
+ * so a request that arrives while others run starts as soon as memory and a
+ * slot free up.  All reductions are fixed-order block sums: a request's
+ * results are bit-identical alone and in any mix.  The server object is
+ * internally synchronised; its calls may come from any thread.
+ * ------------------------------------------------------------------------ */
+typedef struct qms_server qms_server;
+
+typedef struct {
+    double budget_bytes;     /* HBM admission budget (bytes) */
+    int max_resident;        /* concurrently resident solves */
+    int device;
+} qms_srv_desc;
+
+enum { QMS_KEEP_NONE = 0, QMS_KEEP_SLICES = 1 };
+enum { QMS_EXC_NONE = 0, QMS_EXC_COS = 1, QMS_EXC_SIN = 2 };
+
+typedef struct {
+    int xs, ys, zs;
+    double dx, dy, dz, dt;
+    int nt;                  /* transient steps after the steady state (inputs.txt line 4) */
+    int tt;                  /* slice record every tt steps (line 5) */
+    int slice_axis;          /* 0 = x, 1 = y, 2 = z (line 6) */
+    int slice_index;         /* 1-based */
+    int keep;                /* QMS_KEEP_NONE or QMS_KEEP_SLICES */
+    int precision;           /* QMS_PREC_* */
+    double B[3];             /* background field (line 8) */
+    double G[9];             /* its gradient, row-major (lines 9-11) */
+    double traj[3][3];       /* per axis: v0, acceleration, n_acc of trajectory type 1 (line 12) */
+    int exc_kind;            /* QMS_EXC_*: B and G scaled by cos/sin(2 pi f t + phase) */
+    double exc_f, exc_phase;
+    const double* geom;      /* xs*ys*zs float64 material IDs, Fortran order (copied at submit) */
+    const double* table;     /* nmat x 7: ID, mu_r xyz, sigma xyz (copied at submit) */
+    int nmat;
+} qms_request;
+
+enum { QMS_SRV_QUEUED = 0, QMS_SRV_RUNNING = 1, QMS_SRV_DONE = 2, QMS_SRV_FAILED = 3, QMS_SRV_REJECTED = 4 };
+
+typedef struct {
+    int state;               /* QMS_SRV_* */
+    int rc;                  /* the failing call's return code (QMS_ERR_*) or 0 */
+    long long n_dims;
+    int steps_done;          /* transient steps completed */
+    double arrival_s, admitted_s, finished_s;   /* seconds since the server was created */
+    double steady_s;         /* steady-state solve */
+    double step_mean_s, step_max_s;
+    long long n_slice_values; /* values held by qms_srv_slices */
+} qms_srv_result;
+
+typedef struct {
+    long long submitted, completed, failed, rejected;
+    double step_p50_ms, step_p99_ms;             /* per transient step */
+    double request_p50_s, request_p99_s;         /* arrival to finish */
+    double queue_wait_p50_s, queue_wait_p99_s;   /* arrival to admission */
+    double dof_timesteps;                        /* n_dims x steps over completed requests */
+    double wall_s;                               /* first arrival to last finish */
+    double peak_bytes;
+    int peak_resident;
+} qms_srv_stats;
+
+int qms_srv_create(const qms_srv_desc* d, qms_server** out);
+/* Queue a request (inputs are copied; the call returns at once).  A request whose
+ * footprint exceeds the whole budget is recorded as QMS_SRV_REJECTED. */
+int qms_srv_submit(qms_server* s, const qms_request* r, long long* id);
+int qms_srv_poll(qms_server* s, long long id, qms_srv_result* out);      /* non-blocking */
+int qms_srv_wait(qms_server* s, long long id, qms_srv_result* out);      /* until done, failed or rejected */
+/* The slice records of a finished request (steady state, then every tt steps),
+ * each the three components (Hx, Hy, Hz) of the slice back to back.  Copies at
+ * most `cap` values; returns the number copied or a negative error. */
+long long qms_srv_slices(qms_server* s, long long id, double* out, long long cap);
+const char* qms_srv_error(qms_server* s, long long id);
+int qms_srv_stats_get(qms_server* s, qms_srv_stats* out);
+/* Waits for every queued and running request, then frees the server. */
+void qms_srv_destroy(qms_server* s);
 
 #ifdef __cplusplus
 }

@@ -67,3 +67,35 @@ def test_create_without_gpu_fails_cleanly(lib):
     rc = lib.qms_create(ctypes.byref(d), ctypes.byref(h))
     assert rc < 0 and not h.value
     assert lib.qms_last_error(None)
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every struct of include/qms.h has the same size and field offsets in C (compiled
+    here with gcc) as its ctypes mirror in alpineqms_gb300/_lib.py."""
+    import shutil
+    import subprocess
+    from alpineqms_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qms.h"', "int main(void) {"]
+    for name, ct in _lib.STRUCTS.items():
+        lines.append(f'printf("{name} size %zu\\n", sizeof({name}));')
+        for fname, _ in ct._fields_:
+            lines.append(f'printf("{name} {fname} %zu\\n", offsetof({name}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True,
+                   capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            a, b, c = ln.split()
+            got[(a, b)] = int(c)
+    for name, ct in _lib.STRUCTS.items():
+        assert got[(name, "size")] == ctypes.sizeof(ct), name
+        for fname, _ in ct._fields_:
+            assert got[(name, fname)] == getattr(ct, fname).offset, (name, fname)

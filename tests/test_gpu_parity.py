@@ -275,3 +275,39 @@ def test_plain_block_32_twenty_steps(precision):
         xa = s.get_state()[:o.block_offsets(inp.xs, inp.ys, inp.zs)[3]]
         assert abs(np.linalg.norm(xa) - z["anorm"][n]) <= 1e-8 * z["anorm"][n]
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_random_inclusions_32_vs_oracle(precision):
+    """24 random ellipsoids (mu_r up to 1e3, sigma 1e5..6e7) at 32^3, steady + 5 steps: every
+    z-mid H slice, the A and H norms and the edge-current norm within 1e-8 of the oracle's
+    direct solve, and the final A and sigma * grad V within 1e-8 (tests/golden/inclusions_32.npz,
+    made by tests/golden/make_inclusions.py).  Bodies attached to others through a few edges
+    make this the hard case for the potential block."""
+    from alpineqms_gb300 import workloads
+    from alpineqms_gb300.trajectory import VelocitySchedule, scaled_field
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "inclusions_32.npz"))
+    inp, geom = workloads.inclusions_96(seed=2, nt=5, size=32)
+    c = o.materials(inp.xs, inp.ys, inp.zs, geom, inp.props_table())
+    oV = o.block_offsets(inp.xs, inp.ys, inp.zs)[3]
+    sched = VelocitySchedule(inp.traj, inp.dt)
+    s = solver_for(inp.xs, inp.ys, inp.zs, (inp.dx, inp.dy, inp.dz), inp.dt, geom, inp.props_table(),
+                   precision=precision)
+    sl = int(z["slice_index"]) - 1
+    for n in range(0, inp.nt + 1):
+        B, G = scaled_field(inp.B, inp.G, inp.excitation, n * inp.dt)
+        st = s.steady(sched.steady(), B, G) if n == 0 else s.step(sched.step(n), B, G)
+        assert st["status"] == 0, (n, st)
+        H = s.fields()
+        got = np.stack([h.reshape((inp.xs, inp.ys, inp.zs), order="F")[:, :, sl] for h in H])
+        assert rel_l2(got, z["slices"][n]) <= 1e-8, (n, rel_l2(got, z["slices"][n]))
+        hn = np.sqrt(sum(np.dot(h.ravel(), h.ravel()) for h in H))
+        assert abs(hn - z["hnorm"][n]) <= 1e-8 * z["hnorm"][n], (n, hn, z["hnorm"][n])
+        x = s.get_state()
+        assert abs(np.linalg.norm(x[:oV]) - z["anorm"][n]) <= 1e-8 * z["anorm"][n]
+        jn = np.linalg.norm(o.edge_current_from_v(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, c, x))
+        assert abs(jn - z["jnorm"][n]) <= 1e-8 * max(z["jnorm"][n], 1e-300) + 1e-300, (n, jn, z["jnorm"][n])
+    assert rel_l2(x[:oV], z["a_last"]) <= 1e-8, rel_l2(x[:oV], z["a_last"])
+    j = o.edge_current_from_v(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, c, x)
+    assert rel_l2(j, z["j_last"]) <= 1e-8, rel_l2(j, z["j_last"])
+    s.close()

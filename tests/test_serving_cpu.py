@@ -89,3 +89,33 @@ def test_failure_is_isolated():
     rep = latency_report(res, wall=1.0)
     assert rep["completed"] == 2 and rep["failed"] == 1
     assert rep["step_p50_ms"] == pytest.approx(10.0)
+
+
+def test_native_scheduler_without_gpu():
+    """The native serving object (qms_srv_*) on a host without a GPU: every admitted
+    request ends FAILED with the create error (none hangs), a request larger than the
+    whole budget is REJECTED at submit, the stats count both, and destroy returns."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("runs where qms_create cannot succeed")
+    from alpineqms_gb300 import build, workloads
+    from alpineqms_gb300.serving import NativeServer
+    build.build()
+    rng = np.random.default_rng(3)
+    small = [workloads.serving_request(rng, sizes=((16, 16, 16),), nt=2) for _ in range(5)]
+    big = workloads.serving_request(rng, sizes=((128, 128, 128),), nt=2)
+    from alpineqms_gb300.solver import default_desc, device_bytes
+    i0 = small[0][0]
+    fp_small = device_bytes(default_desc(i0.xs, i0.ys, i0.zs, i0.dx, i0.dy, i0.dz, i0.dt))
+    with NativeServer(budget_bytes=3 * fp_small, max_resident=2) as srv:
+        reqs = [SolveRequest(inp, geom) for inp, geom in small] + [SolveRequest(*big)]
+        res = srv.serve(reqs)
+        st = srv.stats()
+    assert [r.status for r in res] == ["failed"] * 5 + ["rejected"]
+    assert all("qms_create" in r.error for r in res[:5])
+    assert st["submitted"] == 6 and st["failed"] == 5 and st["rejected"] == 1 and st["completed"] == 0
+    assert 1 <= st["peak_resident"] <= 2
+    assert st["peak_bytes"] <= 3 * fp_small
+    # admission in arrival order
+    adm = [r.admitted for r in res[:5]]
+    assert adm == sorted(adm)

@@ -29,3 +29,22 @@ def test_alone_vs_mix_bit_identical():
     assert len(again.slices) == len(alone.slices) == 5
     for a, b in zip(alone.slices, again.slices):
         assert np.array_equal(a, b)
+
+
+def test_native_server_matches_python_backend():
+    """The native serving object and the Python scheduler run the same call sequence on
+    the library: a request's slice records are bit-identical through either, alone and
+    in a mix."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from alpineqms_gb300.serving import Backend, NativeServer, QMSServer
+    ref = QMSServer(budget_bytes=8 << 30, max_resident=1, backend=Backend()).serve([_req(21, (24, 20, 16))])[0]
+    assert ref.status == "ok", ref.error
+    with NativeServer(budget_bytes=8 << 30, max_resident=3) as srv:
+        res = srv.serve([_req(22, (20, 20, 20)), _req(21, (24, 20, 16)), _req(23, (16, 24, 20))])
+        st = srv.stats()
+    assert all(r.status == "ok" for r in res), [r.error for r in res]
+    assert len(res[1].slices) == len(ref.slices) == 5
+    for a, b in zip(res[1].slices, ref.slices):
+        assert np.array_equal(a, b)
+    assert st["completed"] == 3 and st["peak_resident"] >= 1
