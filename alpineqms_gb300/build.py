@@ -28,6 +28,7 @@ SOURCES = {
     "qms_noalloc.cu": [],
     "qms_capi.cu": [],
     "qms_server.cpp": [],
+    "qms_pl.cu": [],
 }
 
 

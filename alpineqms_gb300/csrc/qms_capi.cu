@@ -35,7 +35,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->xs = xs; d->ys = ys; d->zs = zs;
     d->dx = dx; d->dy = dy; d->dz = dz; d->dt = dt;
     d->precision = QMS_PREC_MIXED;
-    d->tol = 1e-12;
+    d->tol = 2e-13;
     d->max_outer = 60;
     d->max_inner = 500;
     d->inner_rtol = 1e-3;
@@ -46,7 +46,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->mg_omega = 0.8;
     d->mg_vshift = 0.0;
     d->krylov = QMS_KRYLOV_GMRES;
-    d->gmres_m = 24;
+    d->gmres_m = 32;
     d->use_graphs = 1;
     d->mg_region_cut = 0.0;
 }

@@ -94,7 +94,7 @@ struct QCoef {
     const QMatTable<T>* __restrict__ tab;
     T imu0;
     // optional: the six node coefficients (1/mu_x, 1/mu_y, 1/mu_z, sigma_x, sigma_y, sigma_z)
-    // formed once per geometry, structure of arrays of Nn entries each
+    // formed once per geometry, six arrays in the padded node layout of qms_tma.cuh
     const T* __restrict__ nc = nullptr;
 
     __device__ __forceinline__ int cell(int i, int j, int k) const { return __ldg(id + qCELL(g, i, j, k)); }
@@ -196,4 +196,5 @@ enum QStatusBits : unsigned {
     QMS_ST_NAN = 2u,            // non-finite residual
     QMS_ST_NO_CONVERGENCE = 4u, // iteration limit reached
     QMS_ST_BREAKDOWN = 8u,      // Krylov breakdown (zero denominator)
+    QMS_ST_TIMEOUT = 16u,       // a bounded wait for a tile copy gave up
 };

@@ -93,23 +93,6 @@ __device__ __forceinline__ bool mg_fine_active(const QGrid& g, int b, int i, int
     return b == 0 ? !qFixX(g, i, j, k) : b == 1 ? !qFixY(g, i, j, k) : b == 2 ? !qFixZ(g, i, j, k) : !qFixV(g, i, j, k);
 }
 
-template <typename T>
-__global__ void mg_fine_coef(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, MGLevelDev<T> L) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= L.total) return;
-    const int b = find_block(L, t);
-    const MGBlockDesc& B = L.blk[b];
-    long long q = t - B.off;
-    const int i = (int)(q % B.n1) + 1;
-    const int j = (int)((q / B.n1) % B.n2) + 1;
-    const int k = (int)(q / ((long long)B.n1 * B.n2)) + 1;
-    T w1, w2, w3, d;
-    const bool active = mg_fine_point(g, c, P, vshift, b, i, j, k, w1, w2, w3, d);
-    L.w1[t] = w1; L.w2[t] = w2; L.w3[t] = w3;
-    L.dg[t] = d;                              // diagonal (including links to Dirichlet points)
-    L.dinv[t] = active ? T(1) / d : T(0);     // 0 marks an inactive (Dirichlet) point
-}
-
 // -------------------------------------------------------------- coarsening
 // coarse point (I,J,K) aggregates fine points (2I..2I+1, 2J..2J+1, 2K..2K+1) (0-based):
 // a coarse link is the sum of the fine links crossing between two aggregates, a
@@ -326,18 +309,51 @@ __device__ __forceinline__ T mg_rcp(T d) {
 
 template <typename T, int KIND>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
-mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __restrict__ b,
-          const float* __restrict__ bscale, const T* __restrict__ xin, T* __restrict__ xout, MGLevelDev<T> C,
-          T* __restrict__ bc) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileCoef<T>& tc = *reinterpret_cast<TileCoef<T>*>(smem_raw);
-    XTile<T>& xt = *reinterpret_cast<XTile<T>*>(smem_raw + sizeof(TileCoef<T>));
+mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __restrict__ b, int scaled,
+          const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap, T* __restrict__ xout,
+          MGLevelDev<T> C, T* __restrict__ bc, unsigned* __restrict__ err) {
+    using TL = PLTiles<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][4][PLXY][PLX]
+    T* csm = xsm + 4 * TL::XSLOT;                             // [3 slots][6][PLCY][PLX]
+    __shared__ __align__(8) uint64_t xbar[4], cbar[3];
     __shared__ T red[KIND == 2 ? 4 : 1][OTY][OTX];
     constexpr bool STAGE = KIND != 0;
+    const int tid = threadIdx.x + OTX * threadIdx.y;
     const int i0 = blockIdx.x * OTX + 1, j0 = blockIdx.y * OTY + 1, k0 = blockIdx.z * OKB + 1;
     const int li = threadIdx.x + 1, lj = threadIdx.y + 1;
     const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
     const bool inij = i <= g.Nx && j <= g.Ny;
+    const int kend = min(k0 + OKB - 1, g.Nz);
+    const QPL L = qms_pl(g);
+    const int cx = i0 - 1, cy = j0 - 2;
+    auto issue_x = [&](int kk) {
+        const int sl = kk & 3;
+        mbar_expect_tx(&xbar[sl], TL::XBYTES);
+        tma_load_4d(xsm + sl * TL::XSLOT, &xmap, cx, cy, kk - 1, 0, &xbar[sl]);
+    };
+    auto issue_c = [&](int kk) {
+        const int sl = kk % 3;
+        mbar_expect_tx(&cbar[sl], TL::CBYTES);
+        tma_load_4d(csm + sl * TL::CSLOT, &cmap, cx, cy, kk - 1, 0, &cbar[sl]);
+    };
+    auto xpar = [&](int kk) { return (unsigned)(((kk - (k0 - 1)) >> 2) & 1); };
+    auto cpar = [&](int kk) { return (unsigned)(((kk - (k0 - 1)) / 3) & 1); };
+    if (tid == 0) {
+        for (int q = 0; q < 4; q++) mbar_init(&xbar[q], 1);
+        for (int q = 0; q < 3; q++) mbar_init(&cbar[q], 1);
+        fence_mbar_init();
+        if (STAGE) {
+            issue_x(k0 - 1);
+            issue_x(k0);
+            issue_x(k0 + 1);
+        }
+        issue_c(k0 - 1);
+        issue_c(k0);
+    }
+    __syncthreads();
+    bool ok = mbar_wait(&cbar[(k0 - 1) % 3], cpar(k0 - 1), err);
+    if (STAGE) ok = ok && mbar_wait(&xbar[(k0 - 1) & 3], xpar(k0 - 1), err) && mbar_wait(&xbar[k0 & 3], xpar(k0), err);
     // per-thread parts of the component predicates (qFixX/Y/Z/V without their k terms)
     const bool exX = inij && i <= g.xs, exY = inij && j <= g.ys;
     const bool fxA = i <= 2 || i >= g.Nx - 1, fyA = j <= 2 || j >= g.Ny - 1;
@@ -345,58 +361,54 @@ mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, con
     const bool fijY = fxA || j == 1 || j == g.ys;
     const bool fijZ = fxA || fyA;
     const bool fijV = fxA || fyA || mask_v;
-    const int sXk = g.xs * g.Ny, sYk = g.Nx * g.ys, sZk = g.Nx * g.Ny;
-    // row of each component at plane k0 (32-bit: n_dims < 2^31 is checked at creation)
-    int rX = (i - 1) + (j - 1) * g.xs + (k0 - 1) * sXk;
-    int rY = (int)g.oY + (i - 1) + (j - 1) * g.Nx + (k0 - 1) * sYk;
-    int rZ = (int)g.oZ + (i - 1) + (j - 1) * g.Nx + (k0 - 1) * sZk;
-    int rV = (int)g.oV + (i - 1) + (j - 1) * g.Nx + (k0 - 1) * sZk;
-    const T iscV = bscale ? T(1) / (T(1) + vshift) : T(1);
+    // node offset at plane k0 (padded layout); block q's row is q * comp + node
+    long long nd = inij ? qms_pl_node(g, L, i, j, k0) : 0;
+    const long long plane = (long long)g.Ny * L.P;
+    const T iscV = scaled ? T(1) / (T(1) + vshift) : T(1);
     T acc[4] = {T(0), T(0), T(0), T(0)};
-    const int kend = min(k0 + OKB - 1, g.Nz);
-    XStager xsg;
-    CStager csg;
-    if (STAGE) xsg.init(g, i0, j0);
-    csg.init(g, i0, j0);
-    if (STAGE) {
-        xsg.load(g, xin, xt, k0 - 1);
-        xsg.load(g, xin, xt, k0);
-        xsg.load(g, xin, xt, k0 + 1);
-    }
-    csg.load(c, tc, k0 - 1);
-    csg.load(c, tc, k0);
+    // right-hand side of this thread's four rows, fetched one plane ahead so that the loads
+    // are in flight while the previous plane is computed.  The row scaling of the outer
+    // system is the operator's diagonal, which is this level's diagonal d divided by dscale
+    // (1 + vshift on V, 1 on A): it is formed from the staged coefficients, not read.
     T bn0 = T(0), bn1 = T(0), bn2 = T(0), bn3 = T(0);
-    auto fetch_b = [&](int kk, int dX, int dY, int dZ) {
-        bn0 = exX ? __ldg(b + rX + dX) : T(0);
-        bn1 = exY ? __ldg(b + rY + dY) : T(0);
-        bn2 = inij && kk <= g.zs ? __ldg(b + rZ + dZ) : T(0);
-        bn3 = inij && !mask_v ? __ldg(b + rV + dZ) : T(0);
+    auto fetch_b = [&](int kk, long long n) {
+        bn0 = exX ? __ldg(b + n) : T(0);
+        bn1 = exY ? __ldg(b + L.comp + n) : T(0);
+        bn2 = inij && kk <= g.zs ? __ldg(b + 2 * L.comp + n) : T(0);
+        bn3 = inij && !mask_v ? __ldg(b + 3 * L.comp + n) : T(0);
     };
-    fetch_b(k0, 0, 0, 0);
+    fetch_b(k0, nd);
     for (int k = k0; k <= kend; k++) {
         const T b0 = bn0, b1 = bn1, b2 = bn2, b3 = bn3;
-        if (k < kend) fetch_b(k + 1, sXk, sYk, sZk);
-        cp_async_wait_all();
-        __syncthreads();                       // x planes k-1..k+1 and coefficient planes k-1..k ready
-        if (STAGE && k + 2 <= kend + 1) xsg.load(g, xin, xt, k + 2);
-        if (k < kend) csg.load(c, tc, k + 1);
-        const int cur = tslot(k), prv = tslot(k - 1);
-        const int xm = xslot(k - 1), x0 = xslot(k), xp = xslot(k + 1);
+        if (k < kend) fetch_b(k + 1, nd + plane);
+        if (!__syncthreads_and(ok)) break;         // slots of plane k-2 free; uniform stop on a lost copy
+        if (tid == 0) {
+            fence_proxy_async();
+            if (STAGE && k + 2 <= kend + 1) issue_x(k + 2);
+            if (k < kend) issue_c(k + 1);
+        }
+        ok = mbar_wait(&cbar[k % 3], cpar(k), err);
+        if (STAGE) ok = ok && mbar_wait(&xbar[(k + 1) & 3], xpar(k + 1), err);
+        const T* xm = xsm + ((k - 1) & 3) * TL::XSLOT;
+        const T* x0 = xsm + (k & 3) * TL::XSLOT;
+        const T* xp = xsm + ((k + 1) & 3) * TL::XSLOT;
+        const T* cprv = csm + ((k - 1) % 3) * TL::CSLOT;
+        const T* ccur = csm + (k % 3) * TL::CSLOT;
         const bool kfA = k <= 2 || k >= g.Nz - 1;       // k terms of qFixX / qFixY / qFixV
         const bool kfZ = k == 1 || k == g.zs;           // k term of qFixZ
-#define CF(q, s, dj, di) tc.c[s][q][lj + (dj)][li + (di)]
-#define XS(q, sl, dj, di) xt.v[sl][q][lj + (dj)][li + (di)]
+#define CF(q, dk, dj, di) (dk < 0 ? cprv : ccur)[((q) * PLCY + lj + (dj)) * PLX + li + (di)]
+#define XS(q, sl, dj, di) (sl)[((q) * PLXY + lj + (dj)) * PLX + li + (di)]
         T r[4] = {T(0), T(0), T(0), T(0)};
         // one component: links (wxp, wxm, wyp, wym, wzp, wzm), extra diagonal
-        auto point = [&](int q, bool exists, bool fixed, int row, T bq, T wxp, T wxm, T wyp, T wym, T wzp, T wzm,
-                         T dextra, T dscale, T isc) {
+        auto point = [&](int q, bool exists, bool fixed, long long row, T bq, T wxp, T wxm, T wyp, T wym, T wzp,
+                         T wzm, T dextra, T dscale, T isc) {
             if (!exists) return;
             if (fixed) {
                 if (KIND != 2) xout[row] = T(0);
                 return;
             }
             const T d = (wxp + wxm + wyp + wym + wzp + wzm + dextra) * dscale;
-            const T bv = bscale ? bq * d * isc : bq;
+            const T bv = scaled ? bq * d * isc : bq;
             if (KIND == 0) {
                 xout[row] = omega * bv * mg_rcp(d);
                 return;
@@ -410,29 +422,28 @@ mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, con
             if (KIND == 2) r[q] = bv - Ax;
             else xout[row] = xc + omega * (bv - Ax) * mg_rcp(d);
         };
-        point(0, exX, fijX || kfA, rX, b0,
-              CF(0, cur, 0, 0) * P.idx2, CF(0, cur, 0, -1) * P.idx2, CF(2, cur, 0, 0) * P.idy2,
-              CF(2, cur, -1, 0) * P.idy2, CF(1, cur, 0, 0) * P.idz2, CF(1, prv, 0, 0) * P.idz2,
-              CF(3, cur, 0, 0) * P.idt, T(1), T(1));
-        point(1, exY, fijY || kfA, rY, b1,
-              CF(2, cur, 0, 0) * P.idx2, CF(2, cur, 0, -1) * P.idx2, CF(1, cur, 0, 0) * P.idy2,
-              CF(1, cur, -1, 0) * P.idy2, CF(0, cur, 0, 0) * P.idz2, CF(0, prv, 0, 0) * P.idz2,
-              CF(4, cur, 0, 0) * P.idt, T(1), T(1));
-        point(2, inij && k <= g.zs, fijZ || kfZ, rZ, b2,
-              CF(1, cur, 0, 0) * P.idx2, CF(1, cur, 0, -1) * P.idx2, CF(0, cur, 0, 0) * P.idy2,
-              CF(0, cur, -1, 0) * P.idy2, CF(2, cur, 0, 0) * P.idz2, CF(2, prv, 0, 0) * P.idz2,
-              CF(5, cur, 0, 0) * P.idt, T(1), T(1));
+        point(0, exX, fijX || kfA, nd, b0,
+              CF(0, 0, 0, 0) * P.idx2, CF(0, 0, 0, -1) * P.idx2, CF(2, 0, 0, 0) * P.idy2,
+              CF(2, 0, -1, 0) * P.idy2, CF(1, 0, 0, 0) * P.idz2, CF(1, -1, 0, 0) * P.idz2,
+              CF(3, 0, 0, 0) * P.idt, T(1), T(1));
+        point(1, exY, fijY || kfA, L.comp + nd, b1,
+              CF(2, 0, 0, 0) * P.idx2, CF(2, 0, 0, -1) * P.idx2, CF(1, 0, 0, 0) * P.idy2,
+              CF(1, 0, -1, 0) * P.idy2, CF(0, 0, 0, 0) * P.idz2, CF(0, -1, 0, 0) * P.idz2,
+              CF(4, 0, 0, 0) * P.idt, T(1), T(1));
+        point(2, inij && k <= g.zs, fijZ || kfZ, 2 * L.comp + nd, b2,
+              CF(1, 0, 0, 0) * P.idx2, CF(1, 0, 0, -1) * P.idx2, CF(0, 0, 0, 0) * P.idy2,
+              CF(0, 0, -1, 0) * P.idy2, CF(2, 0, 0, 0) * P.idz2, CF(2, -1, 0, 0) * P.idz2,
+              CF(5, 0, 0, 0) * P.idt, T(1), T(1));
         {
             const T fl = P.sigfloor;
-            point(3, inij, fijV || kfA, rV, b3,
-                  fmax(CF(3, cur, 0, 0), fl) * P.idx2, fmax(CF(3, cur, 0, -1), fl) * P.idx2,
-                  fmax(CF(4, cur, 0, 0), fl) * P.idy2, fmax(CF(4, cur, -1, 0), fl) * P.idy2,
-                  fmax(CF(5, cur, 0, 0), fl) * P.idz2, fmax(CF(5, prv, 0, 0), fl) * P.idz2, T(0), T(1) + vshift,
-                  iscV);
+            point(3, inij, fijV || kfA, 3 * L.comp + nd, b3,
+                  fmax(CF(3, 0, 0, 0), fl) * P.idx2, fmax(CF(3, 0, 0, -1), fl) * P.idx2,
+                  fmax(CF(4, 0, 0, 0), fl) * P.idy2, fmax(CF(4, 0, -1, 0), fl) * P.idy2,
+                  fmax(CF(5, 0, 0, 0), fl) * P.idz2, fmax(CF(5, -1, 0, 0), fl) * P.idz2, T(0), T(1) + vshift, iscV);
         }
 #undef CF
 #undef XS
-        rX += sXk; rY += sYk; rZ += sZk; rV += sZk;
+        nd += plane;
         if (KIND == 2) {
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -464,6 +475,7 @@ mg0_tiled(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, T omega, int mask_v, con
 
 // level 0: x += alpha P x_c on the active points (the Dirichlet points of every component,
 // and V when masked, stay zero); one thread per node (i, j, k), its (up to) four unknowns
+// in the padded layout
 template <typename T>
 __global__ void mg0_prolong(QGrid g, int mask_v, T* __restrict__ x, MGLevelDev<T> C, const T* __restrict__ xc,
                             T alpha) {
@@ -474,16 +486,17 @@ __global__ void mg0_prolong(QGrid g, int mask_v, T* __restrict__ x, MGLevelDev<T
         const MGBlockDesc& cb = C.blk[q];
         return xc[cb.off + I + (long long)J * cb.n1 + (long long)K * cb.n1 * cb.n2];
     };
-    const int sXk = g.xs * g.Ny, sYk = g.Nx * g.ys, sZk = g.Nx * g.Ny;
-    if (i <= g.xs && !qFixX(g, i, j, k)) x[(i - 1) + (j - 1) * g.xs + (k - 1) * sXk] += alpha * coarse(0);
-    if (j <= g.ys && !qFixY(g, i, j, k)) x[g.oY + (i - 1) + (j - 1) * g.Nx + (k - 1) * sYk] += alpha * coarse(1);
-    if (k <= g.zs && !qFixZ(g, i, j, k)) x[g.oZ + (i - 1) + (j - 1) * g.Nx + (k - 1) * sZk] += alpha * coarse(2);
-    if (!mask_v && !qFixV(g, i, j, k)) x[g.oV + (i - 1) + (j - 1) * g.Nx + (k - 1) * sZk] += alpha * coarse(3);
+    const QPL L = qms_pl(g);
+    const long long nd = qms_pl_node(g, L, i, j, k);
+    if (i <= g.xs && !qFixX(g, i, j, k)) x[nd] += alpha * coarse(0);
+    if (j <= g.ys && !qFixY(g, i, j, k)) x[L.comp + nd] += alpha * coarse(1);
+    if (k <= g.zs && !qFixZ(g, i, j, k)) x[2 * L.comp + nd] += alpha * coarse(2);
+    if (!mask_v && !qFixV(g, i, j, k)) x[3 * L.comp + nd] += alpha * coarse(3);
 }
 
 template <typename T, int KIND>
 static size_t mg0_smem() {
-    return sizeof(TileCoef<T>) + (KIND != 0 ? sizeof(XTile<T>) : 0);
+    return PLTiles<T>::SMEM;
 }
 
 // raise the dynamic shared-memory limit of the level-0 kernels once per device
@@ -574,6 +587,19 @@ void QmsMG<T>::release() {
 }
 
 template <typename T>
+int QmsMG<T>::levels_for(const QGrid& g, int min_coarse) {
+    int dims[4][3] = {{g.xs, g.Ny, g.Nz}, {g.Nx, g.ys, g.Nz}, {g.Nx, g.Ny, g.zs}, {g.Nx, g.Ny, g.Nz}};
+    int n = 0;
+    for (;;) {
+        n++;
+        int mx = 0;
+        for (int b = 0; b < 4; b++) mx = std::max({mx, dims[b][0], dims[b][1], dims[b][2]});
+        if (mx <= min_coarse || n >= 12) return n;
+        for (int b = 0; b < 4; b++) for (int a = 0; a < 3; a++) dims[b][a] = (dims[b][a] + 1) / 2;
+    }
+}
+
+template <typename T>
 size_t QmsMG<T>::bytes_for(const QGrid& g, int min_coarse, bool tiled) {
     // every level stores 8 values per point; a tiled level 0 (stored node coefficients,
     // more than one level) stores none: its x/b are the Krylov vectors and the caller's temporary
@@ -620,6 +646,11 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
     // With stored node coefficients level 0 runs on node tiles (mg0_tiled) and level 1 is
     // coarsened straight from the coefficients: level 0 keeps no arrays.
     tiled0 = lv.size() > 1 && c.nc != nullptr;
+    if (!tiled0) {
+        err = "multigrid needs at least two levels and stored node coefficients";
+        release();
+        return -1;
+    }
     for (size_t l = tiled0 ? 1 : 0; l < lv.size(); l++) {
         MGLevelDev<T>& L = lv[l];
         const size_t bytes = L.total * sizeof(T);
@@ -630,12 +661,8 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
     g0 = g; c0 = c; P0 = P; vshift0 = vshift;
     g0block = dim3(OTX, OTY, 1);
     g0grid = dim3((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
-    if (tiled0) {
-        mg_coarsen_fine<<<nblk(lv[1].total), 256, 0, st>>>(g, c, P, vshift, lv[0], lv[1]);
-        mg_mask_links<<<nblk(lv[1].total), 256, 0, st>>>(lv[1]);
-    } else {
-        mg_fine_coef<<<nblk(lv[0].total), 256, 0, st>>>(g, c, P, vshift, lv[0]);
-    }
+    mg_coarsen_fine<<<nblk(lv[1].total), 256, 0, st>>>(g, c, P, vshift, lv[0], lv[1]);
+    mg_mask_links<<<nblk(lv[1].total), 256, 0, st>>>(lv[1]);
     for (size_t l = tiled0 ? 2 : 1; l < lv.size(); l++) {
         mg_coarsen<<<nblk(lv[l].total), 256, 0, st>>>(lv[l - 1], lv[l]);
         mg_mask_links<<<nblk(lv[l].total), 256, 0, st>>>(lv[l]);
@@ -740,74 +767,73 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
 // z = MG(r): level-0 right-hand side b0 (scaled pointwise by `bscale` when given),
 // result in x0; t0 is a level-0 temporary.  Returns the number of kernel launches.
 template <typename T>
-int QmsMG<T>::vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v, cudaStream_t st) {
+int QmsMG<T>::vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
+                     const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st) {
     int launches = 0;
     const int nl = (int)lv.size();
     const int mv = mask_v ? 1 : 0;
-    const T* noT = nullptr;
-    if (tiled0) mg0_prepare<T>();
-#define MG0(KIND, B, BS, XI, XO, BC)                                                                          \
-    mg0_tiled<T, KIND><<<g0grid, g0block, mg0_smem<T, KIND>(), st>>>(g0, c0, P0, vshift0, omega, mv, B, BS, XI, \
-                                                                       XO, lv[1], BC)
-    for (int l = 0; l < nl; l++) {
+    const int sc = scaled ? 1 : 0;
+    mg0_prepare<T>();
+    struct Buf { T* p; const CUtensorMap* m; };
+    // level-0 sweeps: KIND 0 writes XO from b; KIND 1 reads XI (tile copies) and writes XO;
+    // KIND 2 reads XI and writes the level-1 right-hand side
+#define MG0(KIND, XI, XO, BC)                                                                                     \
+    mg0_tiled<T, KIND><<<g0grid, g0block, mg0_smem<T, KIND>(), st>>>(g0, P0, vshift0, omega, mv, b0, sc, *(XI).m, \
+                                                                       cmap, (XO), lv[1], (BC), err)
+    // level 0: nu1 + nu2 sweeps alternate between x0 and t0 (the prolongation is in place);
+    // start in t0 when that count is even so that the last write lands in x0
+    Buf x{x0, &x0map}, t{t0, &t0map};
+    if ((nu1 + nu2) % 2 == 0) std::swap(x, t);
+    MG0(0, x, x.p, nullptr);
+    launches++;
+    for (int s = 1; s < nu1; s++) {
+        MG0(1, x, t.p, nullptr);
+        std::swap(x, t);
+        launches++;
+    }
+    MG0(2, x, nullptr, lv[1].b);
+    launches++;
+    for (int l = 1; l < nl; l++) {
         MGLevelDev<T>& L = lv[l];
-        const T* b = l == 0 ? b0 : L.b;
-        const float* bs = l == 0 ? bscale : nullptr;
-        T* x = l == 0 ? x0 : L.x;
-        T* t = l == 0 ? t0 : L.t;
         if (l == nl - 1) {
-            mg_dense<<<L.nb, 256, 0, st>>>(L, dminv, dmoff, b, x, mv);
+            mg_dense<<<L.nb, 256, 0, st>>>(L, dminv, dmoff, L.b, L.x, mv);
             launches++;
             break;
         }
-        // On tiled level 0 the prolongation is in place, so level 0 writes nu1 + nu2
-        // times, alternating buffers: start in t0 when that count is even so that the
-        // last write lands in x0.
-        if (l == 0 && tiled0 && ((nu1 + nu2) % 2 == 0)) std::swap(x, t);
-        // pre-smoothing: nu1 Jacobi sweeps from zero; keep the result in x
-        if (l == 0 && tiled0) MG0(0, b, bs, noT, x, nullptr);
-        else mg_smooth0<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, mv);
+        T* xl = L.x;
+        T* tl = L.t;
+        mg_smooth0<<<nblk(L.total), 256, 0, st>>>(L, L.b, nullptr, omega, xl, mv);
         launches++;
         for (int s = 1; s < nu1; s++) {
-            if (l == 0 && tiled0) MG0(1, b, bs, x, t, nullptr);
-            else mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, t, mv);
-            std::swap(x, t);
+            mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, L.b, nullptr, omega, xl, tl, mv);
+            std::swap(xl, tl);
             launches++;
         }
-        if (l == 0) { cur_x0 = x; cur_t0 = t; }
-        else { L.x = x; L.t = t; }
-        if (l == 0 && tiled0) MG0(2, b, bs, x, nullptr, lv[1].b);
-        else mg_restrict<<<nblk(lv[l + 1].total), 256, 0, st>>>(L, b, bs, x, lv[l + 1], lv[l + 1].b, mv);
+        L.x = xl;
+        L.t = tl;
+        mg_restrict<<<nblk(lv[l + 1].total), 256, 0, st>>>(L, L.b, nullptr, xl, lv[l + 1], lv[l + 1].b, mv);
         launches++;
     }
-    for (int l = nl - 2; l >= 0; l--) {
+    for (int l = nl - 2; l >= 1; l--) {
         MGLevelDev<T>& L = lv[l];
-        const T* b = l == 0 ? b0 : L.b;
-        const float* bs = l == 0 ? bscale : nullptr;
-        T* x = l == 0 ? cur_x0 : L.x;
-        T* t = l == 0 ? cur_t0 : L.t;
-        if (l == 0 && tiled0) {
-            // in place: level 0 then writes nu1 + nu2 times, alternating from the buffer chosen above
-            mg0_prolong<T><<<dim3((g0.Nx + 127) / 128, g0.Ny, g0.Nz), 128, 0, st>>>(g0, mv, x, lv[1], lv[1].x, alpha);
-        } else {
-            // untiled: prolongate in place, or out of place when the parity of the nu2
-            // sweeps would leave the level-0 result in the temporary
-            const bool flip = l == 0 && (((nu2 % 2 == 0) ? x : t) != x0);
-            if (flip) {
-                mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, x, t, lv[l + 1], lv[l + 1].x, alpha);
-                std::swap(x, t);
-            } else {
-                mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, x, x, lv[l + 1], lv[l + 1].x, alpha);
-            }
-        }
+        T* xl = L.x;
+        T* tl = L.t;
+        mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, xl, xl, lv[l + 1], lv[l + 1].x, alpha);
         launches++;
         for (int s = 0; s < nu2; s++) {
-            if (l == 0 && tiled0) MG0(1, b, bs, x, t, nullptr);
-            else mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, b, bs, omega, x, t, mv);
-            std::swap(x, t);
+            mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, L.b, nullptr, omega, xl, tl, mv);
+            std::swap(xl, tl);
             launches++;
         }
-        if (l > 0) { L.x = x; L.t = t; }
+        L.x = xl;
+        L.t = tl;
+    }
+    mg0_prolong<T><<<dim3((g0.Nx + 127) / 128, g0.Ny, g0.Nz), 128, 0, st>>>(g0, mv, x.p, lv[1], lv[1].x, alpha);
+    launches++;
+    for (int s = 0; s < nu2; s++) {
+        MG0(1, x, t.p, nullptr);
+        std::swap(x, t);
+        launches++;
     }
 #undef MG0
     return launches;
@@ -1033,10 +1059,12 @@ int QmsRegions::build(const QGrid& g, const uint8_t* slots, const double* rows6,
     hrows.resize(hptr[Kr]);
     hrid.resize(hptr[Kr]);
     std::vector<int> fill(hptr.begin(), hptr.end() - 1);
+    const QPL L = qms_pl(g);                        // rows in the inner solver's padded layout
     for (long long p = 0; p < Nn; p++)
         if (nreg[p] >= 0) {
             const int r = nreg[p];
-            hrows[fill[r]] = (int)(g.oV + p);
+            const int i = (int)(p % Nx) + 1, j = (int)((p / Nx) % Ny) + 1, k = (int)(p / ((long long)Nx * Ny)) + 1;
+            hrows[fill[r]] = (int)(3 * L.comp + qms_pl_node(g, L, i, j, k));
             hrid[fill[r]] = r;
             fill[r]++;
         }

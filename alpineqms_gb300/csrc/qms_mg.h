@@ -1,6 +1,7 @@
 // qms_mg.h -- block-diagonal aggregation multigrid (see qms_mg.cu).
 #pragma once
 #include "qms_internal.h"
+#include "qms_tma.cuh"
 
 #include <algorithm>
 #include <string>
@@ -54,7 +55,11 @@ struct QmsMG {
     void release();
     static size_t bytes_for(const QGrid& g, int min_coarse, bool tiled);
     int build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T vshift, cudaStream_t st);
-    int vcycle(const T* b0, const float* bscale, T* x0, T* t0, bool mask_v, cudaStream_t st);
+    // z = MG(r) on the padded layout: b0 (scaled by the operator diagonal when `scaled`), x0 the
+    // result, t0 a temporary; the tensor maps of x0, t0 and of the node coefficients
+    int vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
+               const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st);
+    static int levels_for(const QGrid& g, int min_coarse);
 };
 
 // Coarse space of the V block spanned by one indicator vector per conductor region (a

@@ -21,6 +21,7 @@
 //   RESID:        [0] += |r_A|^2, [1] += |r_V|^2, [2] += |x_A|^2, [3] += |x_V|^2
 #include "qms_internal.h"
 #include "qms_tile.cuh"
+#include "qms_op_rows.cuh"
 #include <algorithm>
 #include <atomic>
 #include <type_traits>
@@ -64,8 +65,7 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
     const int sZj = g.Nx, sZk = g.Nx * g.Ny;      // Az: (Nx, Ny, zs); V: (Nx, Ny, Nz)
     using RT = typename std::conditional<MODE == QOP_RESID, double, float>::type;
     RT red0 = 0, red1 = 0, red2 = 0, red3 = 0;
-    T xc_center = T(0);
-    auto emit = [&](int row, T acc, T diag, bool is_a) {
+    auto emit = [&](long long row, T acc, T diag, bool is_a, T xc_center) {
         T out;
         if (MODE == QOP_APPLY) out = acc;
         else if (MODE == QOP_SCALED) out = op_div(acc, diag);
@@ -106,166 +106,13 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
         if (k < kend) csg.load(c, tc, k + 1);                // coefficients of plane k+1 into that of k-2
         const int cur = tslot(k), prv = tslot(k - 1);
         const int xm = xslot(k - 1), x0 = xslot(k), xp = xslot(k + 1);
-#define CF(q, s, dj, di) tc.c[s][q][lj + (dj)][li + (di)]
-#define XS(comp, sl, dj, di) xt.v[sl][comp][lj + (dj)][li + (di)]
         if (inij) {
-            // ---------------------------------------------------------------- Ax
-            if (i <= g.xs) {
-                const int row = rX;
-                xc_center = XS(0, x0, 0, 0);
-                if (fijX || kfA) {
-                    emit(row, XS(0, x0, 0, 0), T(1), true);
-                } else {
-                    const T s = CF(3, cur, 0, 0);
-                    const T my_km = CF(1, prv, 0, 0), my_k = CF(1, cur, 0, 0);
-                    const T mz_jm = CF(2, cur, -1, 0), mz_j = CF(2, cur, 0, 0);
-                    const T mx_im = CF(0, cur, 0, -1), mx_i = CF(0, cur, 0, 0);
-                    const T svy = ADV ? s * P.vy : T(0), svz = ADV ? s * P.vz : T(0);
-                    const T d = (mz_j + mz_jm) * P.idy2 + (my_k + my_km) * P.idz2 + (mx_i + mx_im) * P.idx2 + s * P.idt;
-                    // difference form: every coupling pair is applied to a difference of unknowns,
-                    // so the rounding error scales with the variation of x, not with x itself
-                    const T X0 = XS(0, x0, 0, 0);
-                    T acc = s * P.idt * X0;
-                    acc += my_km * P.idz2 * (X0 - XS(0, xm, 0, 0)) + my_k * P.idz2 * (X0 - XS(0, xp, 0, 0));
-                    acc += mz_jm * P.idy2 * (X0 - XS(0, x0, -1, 0)) + mz_j * P.idy2 * (X0 - XS(0, x0, 1, 0));
-                    acc += mx_im * P.idx2 * (X0 - XS(0, x0, 0, -1)) + mx_i * P.idx2 * (X0 - XS(0, x0, 0, 1));
-                    if (ADV) {
-                        acc += svz * P.i2dz * (XS(0, xm, 0, 0) - XS(0, xp, 0, 0));
-                        acc += svy * P.i2dy * (XS(0, x0, -1, 0) - XS(0, x0, 1, 0));
-                    }
-                    acc += (mz_jm * P.idxdy - svy * P.i2dx) * (XS(1, x0, -1, 0) - XS(1, x0, -1, 1));
-                    acc += (mz_j * P.idxdy + svy * P.i2dx) * (XS(1, x0, 0, 1) - XS(1, x0, 0, 0));
-                    acc += (my_km * P.idxdz - svz * P.i2dx) * (XS(2, xm, 0, 0) - XS(2, xm, 0, 1));
-                    acc += (my_k * P.idxdz + svz * P.i2dx) * (XS(2, x0, 0, 1) - XS(2, x0, 0, 0));
-                    acc += s * P.idx * (XS(3, x0, 0, 1) - XS(3, x0, 0, 0));
-                    emit(row, acc, d, true);
-                }
-            }
-            // ---------------------------------------------------------------- Ay
-            if (j <= g.ys) {
-                const int row = rY;
-                xc_center = XS(1, x0, 0, 0);
-                if (fijY || kfA) {
-                    emit(row, XS(1, x0, 0, 0), T(1), true);
-                } else {
-                    const T s = CF(4, cur, 0, 0);
-                    const T mz_im = CF(2, cur, 0, -1), mz_i = CF(2, cur, 0, 0);
-                    const T mx_km = CF(0, prv, 0, 0), mx_k = CF(0, cur, 0, 0);
-                    const T my_jm = CF(1, cur, -1, 0), my_j = CF(1, cur, 0, 0);
-                    const T svx = ADV ? s * P.vx : T(0), svz = ADV ? s * P.vz : T(0);
-                    const T d = (mz_i + mz_im) * P.idx2 + (mx_k + mx_km) * P.idz2 + (my_j + my_jm) * P.idy2 + s * P.idt;
-                    const T Y0 = XS(1, x0, 0, 0);
-                    T acc = s * P.idt * Y0;
-                    acc += mx_km * P.idz2 * (Y0 - XS(1, xm, 0, 0)) + mx_k * P.idz2 * (Y0 - XS(1, xp, 0, 0));
-                    acc += my_jm * P.idy2 * (Y0 - XS(1, x0, -1, 0)) + my_j * P.idy2 * (Y0 - XS(1, x0, 1, 0));
-                    acc += mz_im * P.idx2 * (Y0 - XS(1, x0, 0, -1)) + mz_i * P.idx2 * (Y0 - XS(1, x0, 0, 1));
-                    if (ADV) {
-                        acc += svz * P.i2dz * (XS(1, xm, 0, 0) - XS(1, xp, 0, 0));
-                        acc += svx * P.i2dx * (XS(1, x0, 0, -1) - XS(1, x0, 0, 1));
-                    }
-                    acc += (mz_im * P.idxdy - svx * P.i2dy) * (XS(0, x0, 0, -1) - XS(0, x0, 1, -1));
-                    acc += (mz_i * P.idxdy + svx * P.i2dy) * (XS(0, x0, 1, 0) - XS(0, x0, 0, 0));
-                    acc += (mx_km * P.idydz - svz * P.i2dy) * (XS(2, xm, 0, 0) - XS(2, xm, 1, 0));
-                    acc += (mx_k * P.idydz + svz * P.i2dy) * (XS(2, x0, 1, 0) - XS(2, x0, 0, 0));
-                    acc += s * P.idy * (XS(3, x0, 1, 0) - XS(3, x0, 0, 0));
-                    emit(row, acc, d, true);
-                }
-            }
-            // ---------------------------------------------------------------- Az
-            if (k <= g.zs) {
-                const int row = rZ;
-                xc_center = XS(2, x0, 0, 0);
-                if (fijZ || kfZ) {
-                    emit(row, XS(2, x0, 0, 0), T(1), true);
-                } else {
-                    const T s = CF(5, cur, 0, 0);
-                    const T my_im = CF(1, cur, 0, -1), my_i = CF(1, cur, 0, 0);
-                    const T mx_jm = CF(0, cur, -1, 0), mx_j = CF(0, cur, 0, 0);
-                    const T mz_km = CF(2, prv, 0, 0), mz_k = CF(2, cur, 0, 0);
-                    const T svx = ADV ? s * P.vx : T(0), svy = ADV ? s * P.vy : T(0);
-                    const T d = (my_i + my_im) * P.idx2 + (mx_j + mx_jm) * P.idy2 + (mz_k + mz_km) * P.idz2 + s * P.idt;
-                    const T Z0 = XS(2, x0, 0, 0);
-                    T acc = s * P.idt * Z0;
-                    acc += mz_km * P.idz2 * (Z0 - XS(2, xm, 0, 0)) + mz_k * P.idz2 * (Z0 - XS(2, xp, 0, 0));
-                    acc += mx_jm * P.idy2 * (Z0 - XS(2, x0, -1, 0)) + mx_j * P.idy2 * (Z0 - XS(2, x0, 1, 0));
-                    acc += my_im * P.idx2 * (Z0 - XS(2, x0, 0, -1)) + my_i * P.idx2 * (Z0 - XS(2, x0, 0, 1));
-                    if (ADV) {
-                        acc += svy * P.i2dy * (XS(2, x0, -1, 0) - XS(2, x0, 1, 0));
-                        acc += svx * P.i2dx * (XS(2, x0, 0, -1) - XS(2, x0, 0, 1));
-                    }
-                    acc += (my_im * P.idxdz - svx * P.i2dz) * (XS(0, x0, 0, -1) - XS(0, xp, 0, -1));
-                    acc += (my_i * P.idxdz + svx * P.i2dz) * (XS(0, xp, 0, 0) - XS(0, x0, 0, 0));
-                    acc += (mx_jm * P.idydz - svy * P.i2dz) * (XS(1, x0, -1, 0) - XS(1, xp, -1, 0));
-                    acc += (mx_j * P.idydz + svy * P.i2dz) * (XS(1, xp, 0, 0) - XS(1, x0, 0, 0));
-                    acc += s * P.idz * (XS(3, xp, 0, 0) - XS(3, x0, 0, 0));
-                    emit(row, acc, d, true);
-                }
-            }
-            // ---------------------------------------------------------------- V
-            {
-                const int row = rV;
-                xc_center = XS(3, x0, 0, 0);
-                if (fijZ || kfA) {
-                    emit(row, XS(3, x0, 0, 0), T(1), false);
-                } else {
-                    const T sx0 = CF(3, cur, 0, 0), sx1 = CF(3, cur, 0, -1);
-                    const T sy0 = CF(4, cur, 0, 0), sy1 = CF(4, cur, -1, 0);
-                    const T sz0 = CF(5, cur, 0, 0), sz1 = CF(5, prv, 0, 0);
-                    const T fx0 = fmax(sx0, P.sigfloor), fx1 = fmax(sx1, P.sigfloor);
-                    const T fy0 = fmax(sy0, P.sigfloor), fy1 = fmax(sy1, P.sigfloor);
-                    const T fz0 = fmax(sz0, P.sigfloor), fz1 = fmax(sz1, P.sigfloor);
-                    const T d = (fx0 + fx1) * P.idx2 + (fy0 + fy1) * P.idy2 + (fz0 + fz1) * P.idz2;
-                    const T V0 = XS(3, x0, 0, 0);
-                    T acc = fz1 * P.idz2 * (V0 - XS(3, xm, 0, 0)) + fz0 * P.idz2 * (V0 - XS(3, xp, 0, 0));
-                    acc += fy1 * P.idy2 * (V0 - XS(3, x0, -1, 0)) + fy0 * P.idy2 * (V0 - XS(3, x0, 1, 0));
-                    acc += fx1 * P.idx2 * (V0 - XS(3, x0, 0, -1)) + fx0 * P.idx2 * (V0 - XS(3, x0, 0, 1));
-                    const T axm = XS(0, x0, 0, -1), ax0 = XS(0, x0, 0, 0);
-                    const T aym = XS(1, x0, -1, 0), ay0 = XS(1, x0, 0, 0);
-                    const T azm = XS(2, xm, 0, 0), az0 = XS(2, x0, 0, 0);
-                    // div(sigma A) / dt: s0 a0 - s1 a1 = s0 (a0 - a1) + (s0 - s1) a1 (exact inside a body)
-                    acc += P.idt * ((sx0 * (ax0 - axm) + (sx0 - sx1) * axm) * P.idx +
-                                    (sy0 * (ay0 - aym) + (sy0 - sy1) * aym) * P.idy +
-                                    (sz0 * (az0 - azm) + (sz0 - sz1) * azm) * P.idz);
-                    if (ADV) {
-                        // div(sigma v x curl A), grouped by velocity component into differences
-                        const T vx = P.vx, vy = P.vy, vz = P.vz;
-                        // Ax neighbours
-                        const T SA = axm + ax0;
-                        acc += vz * P.i2dxdz * (sx1 * (XS(0, xm, 0, -1) - XS(0, xp, 0, -1)) +
-                                                 sx0 * (XS(0, xp, 0, 0) - XS(0, xm, 0, 0)));
-                        acc += vy * P.i2dxdy * (sx1 * (XS(0, x0, -1, -1) - XS(0, x0, 1, -1)) +
-                                                 sx0 * (XS(0, x0, 1, 0) - XS(0, x0, -1, 0)));
-                        acc += vx * P.i2dy2 * (sy1 * (SA - (XS(0, x0, -1, -1) + XS(0, x0, -1, 0))) +
-                                               sy0 * (SA - (XS(0, x0, 1, -1) + XS(0, x0, 1, 0))));
-                        acc += vx * P.i2dz2 * (sz1 * (SA - (XS(0, xm, 0, -1) + XS(0, xm, 0, 0))) +
-                                               sz0 * (SA - (XS(0, xp, 0, -1) + XS(0, xp, 0, 0))));
-                        // Ay neighbours
-                        const T SB = aym + ay0;
-                        acc += vz * P.i2dydz * (sy1 * (XS(1, xm, -1, 0) - XS(1, xp, -1, 0)) +
-                                                 sy0 * (XS(1, xp, 0, 0) - XS(1, xm, 0, 0)));
-                        acc += vx * P.i2dxdy * (sy1 * (XS(1, x0, -1, -1) - XS(1, x0, -1, 1)) +
-                                                 sy0 * (XS(1, x0, 0, 1) - XS(1, x0, 0, -1)));
-                        acc += vy * P.i2dx2 * (sx1 * (SB - (XS(1, x0, -1, -1) + XS(1, x0, 0, -1))) +
-                                               sx0 * (SB - (XS(1, x0, -1, 1) + XS(1, x0, 0, 1))));
-                        acc += vy * P.i2dz2 * (sz1 * (SB - (XS(1, xm, -1, 0) + XS(1, xm, 0, 0))) +
-                                               sz0 * (SB - (XS(1, xp, -1, 0) + XS(1, xp, 0, 0))));
-                        // Az neighbours
-                        const T SC = azm + az0;
-                        acc += vy * P.i2dydz * (sz1 * (XS(2, xm, -1, 0) - XS(2, xm, 1, 0)) +
-                                                 sz0 * (XS(2, x0, 1, 0) - XS(2, x0, -1, 0)));
-                        acc += vx * P.i2dxdz * (sz1 * (XS(2, xm, 0, -1) - XS(2, xm, 0, 1)) +
-                                                 sz0 * (XS(2, x0, 0, 1) - XS(2, x0, 0, -1)));
-                        acc += vz * P.i2dx2 * (sx1 * (SC - (XS(2, xm, 0, -1) + XS(2, x0, 0, -1))) +
-                                               sx0 * (SC - (XS(2, xm, 0, 1) + XS(2, x0, 0, 1))));
-                        acc += vz * P.i2dy2 * (sy1 * (SC - (XS(2, xm, -1, 0) + XS(2, x0, -1, 0))) +
-                                               sy0 * (SC - (XS(2, xm, 1, 0) + XS(2, x0, 1, 0))));
-                    }
-                    emit(row, acc, d, false);
-                }
-            }
+            auto xsf = [&](int comp, int dk, int dj, int di) -> T {
+                return xt.v[dk < 0 ? xm : (dk > 0 ? xp : x0)][comp][lj + dj][li + di];
+            };
+            auto cff = [&](int q, int dk, int dj, int di) -> T { return tc.c[dk < 0 ? prv : cur][q][lj + dj][li + di]; };
+            qms_op_node<T, ADV>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, rY, rZ, rV, xsf, cff, emit);
         }
-#undef CF
-#undef XS
         rX += sXk; rY += sYk; rZ += sZk; rV += sZk;
     }
     if (partials) {
@@ -288,15 +135,16 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
 // The six node coefficients, formed once per geometry from the material slots.
 template <typename T>
 __global__ void qk_node_coef(QGrid g, QCoef<T> c, T* __restrict__ nc) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.Nn) return;
-    const int i = (int)(t % g.Nx) + 1, j = (int)((t / g.Nx) % g.Ny) + 1, k = (int)(t / ((long long)g.Nx * g.Ny)) + 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > g.Nx) return;
+    const QPL L = qms_pl(g);
+    const long long t = qms_pl_node(g, L, i, j, k);
     nc[t] = c.imux(i, j, k);
-    nc[g.Nn + t] = c.imuy(i, j, k);
-    nc[2 * g.Nn + t] = c.imuz(i, j, k);
-    nc[3 * g.Nn + t] = c.sgx(i, j, k);
-    nc[4 * g.Nn + t] = c.sgy(i, j, k);
-    nc[5 * g.Nn + t] = c.sgz(i, j, k);
+    nc[L.comp + t] = c.imuy(i, j, k);
+    nc[2 * L.comp + t] = c.imuz(i, j, k);
+    nc[3 * L.comp + t] = c.sgx(i, j, k);
+    nc[4 * L.comp + t] = c.sgy(i, j, k);
+    nc[5 * L.comp + t] = c.sgz(i, j, k);
 }
 
 // Diagonal of the (steady or transient) operator, FP32, for the Jacobi
@@ -410,7 +258,9 @@ template <typename T>
 void qms_launch_node_coef(const QGrid& g, const QCoef<T>& c, T* nc, cudaStream_t st) {
     QCoef<T> c0 = c;
     c0.nc = nullptr;
-    qk_node_coef<T><<<(unsigned)((g.Nn + 255) / 256), 256, 0, st>>>(g, c0, nc);
+    // padding between and around the nodes stays zero
+    cudaMemsetAsync(nc, 0, 6 * qms_pl(g).comp * sizeof(T), st);
+    qk_node_coef<T><<<dim3((g.Nx + 127) / 128, g.Ny, g.Nz), 128, 0, st>>>(g, c0, nc);
 }
 template void qms_launch_node_coef<float>(const QGrid&, const QCoef<float>&, float*, cudaStream_t);
 template void qms_launch_node_coef<double>(const QGrid&, const QCoef<double>&, double*, cudaStream_t);

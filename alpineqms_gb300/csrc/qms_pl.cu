@@ -1,0 +1,295 @@
+// qms_pl.cu -- the inner solver's operator on the padded node layout (qms_tma.cuh), its
+// FP32 diagonal, and the maps between that layout and the reference's unknown order.
+//
+// qk_op_pl: one CTA of 32 x 8 threads owns a column of nodes and marches 16 k-planes.  Per
+// plane, one thread issues two cp.async.bulk.tensor copies: the four unknown blocks of
+// plane k+2 (+-1 halo, zero-filled outside the grid) into a four-slot ring, and the six node
+// coefficients of plane k+1 into a three-slot ring, each completing on its own mbarrier.
+// All threads wait (bounded) for the planes they need and evaluate their node's (up to)
+// four rows from shared memory (qms_op_rows.cuh).  The only per-thread global traffic is
+// the output row (and the optional dot vector).
+#include "qms_internal.h"
+#include "qms_op_rows.cuh"
+#include "qms_pl.h"
+#include "qms_tile.cuh"
+
+#include <cudaTypedefs.h>
+#include <atomic>
+#include <mutex>
+
+// ---------------------------------------------------------------------------
+// tensor maps
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+bool qms_make_pl_map(CUtensorMap* map, const void* base, const QGrid& g, int elem_bytes, int arrays, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return false;
+    const QPL L = qms_pl(g);
+    const cuuint64_t dims[4] = {(cuuint64_t)L.P, (cuuint64_t)g.Ny, (cuuint64_t)g.Nz, (cuuint64_t)arrays};
+    const cuuint64_t strides[3] = {(cuuint64_t)L.P * elem_bytes, (cuuint64_t)L.P * g.Ny * elem_bytes,
+                                   (cuuint64_t)L.comp * elem_bytes};
+    const cuuint32_t box[4] = {PLX, (cuuint32_t)box_rows, 1, (cuuint32_t)arrays};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(map, elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                           const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// operator on the padded layout
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T pl_div(T a, T d) {
+    if constexpr (sizeof(T) == 4) return __fdividef(a, d);
+    else return a / d;
+}
+
+// MODE: QOPH_APPLY (y = M x) or QOPH_SCALED (y = D^-1 M x); partials (optional, FP64):
+// [0] += y . w (w may be null), [1] += y . y
+template <typename T, bool ADV, int MODE>
+__global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
+qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap,
+         T* __restrict__ y, const T* __restrict__ w, double* __restrict__ partials, unsigned* __restrict__ err) {
+    using TL = PLTiles<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][4][PLXY][PLX]
+    T* csm = xsm + 4 * TL::XSLOT;                             // [3 slots][6][PLCY][PLX]
+    __shared__ __align__(8) uint64_t xbar[4], cbar[3];
+    const int tid = threadIdx.x + OTX * threadIdx.y;
+    const int i0 = blockIdx.x * OTX + 1, j0 = blockIdx.y * OTY + 1, k0 = blockIdx.z * OKB + 1;
+    const int li = threadIdx.x + 1, lj = threadIdx.y + 1;
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    const bool inij = i <= g.Nx && j <= g.Ny;
+    const int kend = min(k0 + OKB - 1, g.Nz);
+    const QPL L = qms_pl(g);
+    // tile origin in tensor coordinates: column i0 - 1 (a multiple of 32), row j0 - 2 (0-based)
+    const int cx = i0 - 1, cy = j0 - 2;
+    auto issue_x = [&](int kk) {
+        const int sl = kk & 3;
+        mbar_expect_tx(&xbar[sl], TL::XBYTES);
+        tma_load_4d(xsm + sl * TL::XSLOT, &xmap, cx, cy, kk - 1, 0, &xbar[sl]);
+    };
+    auto issue_c = [&](int kk) {
+        const int sl = kk % 3;
+        mbar_expect_tx(&cbar[sl], TL::CBYTES);
+        tma_load_4d(csm + sl * TL::CSLOT, &cmap, cx, cy, kk - 1, 0, &cbar[sl]);
+    };
+    // parity of the use of a ring slot by plane kk (planes k0-1, k0, ... fill the slots in turn)
+    auto xpar = [&](int kk) { return (unsigned)(((kk - (k0 - 1)) >> 2) & 1); };
+    auto cpar = [&](int kk) { return (unsigned)(((kk - (k0 - 1)) / 3) & 1); };
+    if (tid == 0) {
+        for (int q = 0; q < 4; q++) mbar_init(&xbar[q], 1);
+        for (int q = 0; q < 3; q++) mbar_init(&cbar[q], 1);
+        fence_mbar_init();
+        issue_x(k0 - 1);
+        issue_x(k0);
+        issue_x(k0 + 1);
+        issue_c(k0 - 1);
+        issue_c(k0);
+    }
+    __syncthreads();
+    bool ok = mbar_wait(&xbar[(k0 - 1) & 3], xpar(k0 - 1), err) && mbar_wait(&xbar[k0 & 3], xpar(k0), err) &&
+              mbar_wait(&cbar[(k0 - 1) % 3], cpar(k0 - 1), err);
+    // (i, j) parts of the Dirichlet predicates; rows at plane k0 (padded layout)
+    const bool fxA = i <= 2 || i >= g.Nx - 1, fyA = j <= 2 || j >= g.Ny - 1;
+    const bool fijX = fyA || i == 1 || i == g.xs, fijY = fxA || j == 1 || j == g.ys, fijZ = fxA || fyA;
+    long long rX = qms_pl_node(g, L, i, j, k0);
+    const long long plane = (long long)g.Ny * L.P;
+    // per-thread sums in FP32 (the dot vectors of the inner solver are FP32 or FP64 already;
+    // FP64 arithmetic per row would make the kernel FP64-throughput bound), FP64 across warps
+    using RT = float;
+    RT red0 = 0, red1 = 0;
+    auto emit = [&](long long row, T acc, T diag, bool, T) {
+        const T out = MODE == QOPH_APPLY ? acc : pl_div(acc, diag);
+        y[row] = out;
+        if (partials) {
+            if (w) red0 += (RT)(out * w[row]);
+            red1 += (RT)(out * out);
+        }
+    };
+    for (int k = k0; k <= kend; k++) {
+        // all threads are done with plane k-1's slots; a copy that never arrived (flagged in
+        // *err) ends the sweep for the whole CTA at once
+        if (!__syncthreads_and(ok)) break;
+        if (tid == 0) {
+            fence_proxy_async();
+            if (k + 2 <= kend + 1) issue_x(k + 2);   // into the slot of plane k-2
+            if (k < kend) issue_c(k + 1);            // into the slot of plane k-2
+        }
+        ok = mbar_wait(&xbar[(k + 1) & 3], xpar(k + 1), err) && mbar_wait(&cbar[k % 3], cpar(k), err);
+        const T* xm = xsm + ((k - 1) & 3) * TL::XSLOT;
+        const T* x0 = xsm + (k & 3) * TL::XSLOT;
+        const T* xp = xsm + ((k + 1) & 3) * TL::XSLOT;
+        const T* cprv = csm + ((k - 1) % 3) * TL::CSLOT;
+        const T* ccur = csm + (k % 3) * TL::CSLOT;
+        if (inij) {
+            auto xsf = [&](int comp, int dk, int dj, int di) -> T {
+                const T* b = dk < 0 ? xm : (dk > 0 ? xp : x0);
+                return b[(comp * PLXY + lj + dj) * PLX + li + di];
+            };
+            auto cff = [&](int q, int dk, int dj, int di) -> T {
+                return (dk < 0 ? cprv : ccur)[(q * PLCY + lj + dj) * PLX + li + di];
+            };
+            const bool kfA = k <= 2 || k >= g.Nz - 1, kfZ = k == 1 || k == g.zs;
+            qms_op_node<T, ADV>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, L.comp + rX, 2 * L.comp + rX,
+                                3 * L.comp + rX, xsf, cff, emit);
+        }
+        rX += plane;
+    }
+    if (partials) {
+        __shared__ double sh[32];
+        const long long bid = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+        const long long nb = (long long)gridDim.x * gridDim.y * gridDim.z;
+        double s0 = qBlockSum(red0, sh);
+        if (qLinTid() == 0) partials[bid] = s0;
+        double s1 = qBlockSum(red1, sh);
+        if (qLinTid() == 0) partials[nb + bid] = s1;
+    }
+}
+
+// FP32 diagonal of the operator in the padded layout (Dirichlet rows 1)
+__global__ void qk_diag_pl(QGrid g, QCoef<float> c, QStepPar<float> P, float* __restrict__ dg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > g.Nx) return;
+    const QPL L = qms_pl(g);
+    const long long t = qms_pl_node(g, L, i, j, k);
+    if (i <= g.xs) {
+        float d = 1.f;
+        if (!qFixX(g, i, j, k))
+            d = (c.imuz(i, j, k) + c.imuz(i, j - 1, k)) * P.idy2 + (c.imuy(i, j, k) + c.imuy(i, j, k - 1)) * P.idz2 +
+                (c.imux(i, j, k) + c.imux(i - 1, j, k)) * P.idx2 + c.sgx(i, j, k) * P.idt;
+        dg[t] = d;
+    }
+    if (j <= g.ys) {
+        float d = 1.f;
+        if (!qFixY(g, i, j, k))
+            d = (c.imuz(i, j, k) + c.imuz(i - 1, j, k)) * P.idx2 + (c.imux(i, j, k) + c.imux(i, j, k - 1)) * P.idz2 +
+                (c.imuy(i, j, k) + c.imuy(i, j - 1, k)) * P.idy2 + c.sgy(i, j, k) * P.idt;
+        dg[L.comp + t] = d;
+    }
+    if (k <= g.zs) {
+        float d = 1.f;
+        if (!qFixZ(g, i, j, k))
+            d = (c.imuy(i, j, k) + c.imuy(i - 1, j, k)) * P.idx2 + (c.imux(i, j, k) + c.imux(i, j - 1, k)) * P.idy2 +
+                (c.imuz(i, j, k) + c.imuz(i, j, k - 1)) * P.idz2 + c.sgz(i, j, k) * P.idt;
+        dg[2 * L.comp + t] = d;
+    }
+    float d = 1.f;
+    if (!qFixV(g, i, j, k)) {
+        const float f = P.sigfloor;
+        d = (fmaxf(c.sgx(i, j, k), f) + fmaxf(c.sgx(i - 1, j, k), f)) * P.idx2 +
+            (fmaxf(c.sgy(i, j, k), f) + fmaxf(c.sgy(i, j - 1, k), f)) * P.idy2 +
+            (fmaxf(c.sgz(i, j, k), f) + fmaxf(c.sgz(i, j, k - 1), f)) * P.idz2;
+    }
+    dg[3 * L.comp + t] = d;
+}
+
+// out[PL] = (T)(r64[ref] * scale[0])
+template <typename T>
+__global__ void qk_pl_from_ref(QGrid g, const double* __restrict__ r64, const double* __restrict__ scale,
+                               T* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > g.Nx) return;
+    const QPL L = qms_pl(g);
+    const long long t = qms_pl_node(g, L, i, j, k);
+    const double s = scale ? scale[0] : 1.0;
+    if (i <= g.xs) out[t] = (T)(r64[qAX(g, i, j, k)] * s);
+    if (j <= g.ys) out[L.comp + t] = (T)(r64[qAY(g, i, j, k)] * s);
+    if (k <= g.zs) out[2 * L.comp + t] = (T)(r64[qAZ(g, i, j, k)] * s);
+    out[3 * L.comp + t] = (T)(r64[qV(g, i, j, k)] * s);
+}
+
+// x[ref] += scale[0] * e[PL]
+template <typename T>
+__global__ void qk_ref_add_pl(QGrid g, const T* __restrict__ e, const double* __restrict__ scale,
+                              double* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > g.Nx) return;
+    const QPL L = qms_pl(g);
+    const long long t = qms_pl_node(g, L, i, j, k);
+    const double s = scale[0];
+    if (i <= g.xs) x[qAX(g, i, j, k)] += s * (double)e[t];
+    if (j <= g.ys) x[qAY(g, i, j, k)] += s * (double)e[L.comp + t];
+    if (k <= g.zs) x[qAZ(g, i, j, k)] += s * (double)e[2 * L.comp + t];
+    x[qV(g, i, j, k)] += s * (double)e[3 * L.comp + t];
+}
+
+}  // namespace
+
+dim3 qms_node_grid(const QGrid& g) { return dim3((g.Nx + 127) / 128, g.Ny, g.Nz); }
+
+template <typename T>
+static void op_pl_prepare() {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    const int shm = (int)PLTiles<T>::SMEM;
+    cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
+long long qms_op_pl_num_blocks(const QGrid& g) {
+    return (long long)((g.Nx + OTX - 1) / OTX) * ((g.Ny + OTY - 1) / OTY) * ((g.Nz + OKB - 1) / OKB);
+}
+
+template <typename T>
+void qms_launch_op_pl(const QGrid& g, const QStepPar<T>& P, const CUtensorMap& xmap, const CUtensorMap& cmap, bool adv,
+                      int mode, T* y, const T* w, double* partials, unsigned* err, cudaStream_t st) {
+    op_pl_prepare<T>();
+    const dim3 bs(OTX, OTY, 1), gs((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
+    const size_t shm = PLTiles<T>::SMEM;
+#define L(ADV, MODE) qk_op_pl<T, ADV, MODE><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err)
+    if (adv) {
+        if (mode == QOPH_APPLY) L(true, QOPH_APPLY);
+        else L(true, QOPH_SCALED);
+    } else {
+        if (mode == QOPH_APPLY) L(false, QOPH_APPLY);
+        else L(false, QOPH_SCALED);
+    }
+#undef L
+}
+template void qms_launch_op_pl<float>(const QGrid&, const QStepPar<float>&, const CUtensorMap&, const CUtensorMap&,
+                                      bool, int, float*, const float*, double*, unsigned*, cudaStream_t);
+template void qms_launch_op_pl<double>(const QGrid&, const QStepPar<double>&, const CUtensorMap&, const CUtensorMap&,
+                                       bool, int, double*, const double*, double*, unsigned*, cudaStream_t);
+
+void qms_launch_diag_pl(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st) {
+    cudaMemsetAsync(dg, 0, qms_pl(g).n * sizeof(float), st);
+    qk_diag_pl<<<qms_node_grid(g), 128, 0, st>>>(g, c, P, dg);
+}
+
+template <typename T>
+void qms_launch_pl_from_ref(const QGrid& g, const double* r64, const double* scale, T* out, cudaStream_t st) {
+    qk_pl_from_ref<T><<<qms_node_grid(g), 128, 0, st>>>(g, r64, scale, out);
+}
+template void qms_launch_pl_from_ref<float>(const QGrid&, const double*, const double*, float*, cudaStream_t);
+template void qms_launch_pl_from_ref<double>(const QGrid&, const double*, const double*, double*, cudaStream_t);
+
+template <typename T>
+void qms_launch_ref_add_pl(const QGrid& g, const T* e, const double* scale, double* x, cudaStream_t st) {
+    qk_ref_add_pl<T><<<qms_node_grid(g), 128, 0, st>>>(g, e, scale, x);
+}
+template void qms_launch_ref_add_pl<float>(const QGrid&, const float*, const double*, double*, cudaStream_t);
+template void qms_launch_ref_add_pl<double>(const QGrid&, const double*, const double*, double*, cudaStream_t);

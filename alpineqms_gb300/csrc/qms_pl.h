@@ -1,0 +1,22 @@
+// qms_pl.h -- launchers of the padded-layout kernels (qms_pl.cu).
+#pragma once
+#include "qms_internal.h"
+#include "qms_tma.cuh"
+
+dim3 qms_node_grid(const QGrid& g);                 // one thread per node: (ceil(Nx/128), Ny, Nz) x 128
+long long qms_op_pl_num_blocks(const QGrid& g);
+
+// y = M x (mode QOPH_APPLY) or D^-1 M x (QOPH_SCALED) on padded vectors; x and the node
+// coefficients come through their tensor maps (qms_make_pl_map, 10 and 9 rows per box)
+template <typename T>
+void qms_launch_op_pl(const QGrid& g, const QStepPar<T>& P, const CUtensorMap& xmap, const CUtensorMap& cmap, bool adv,
+                      int mode, T* y, const T* w, double* partials, unsigned* err, cudaStream_t st);
+
+void qms_launch_diag_pl(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st);
+
+// out[PL] = r64[ref] * scale[0] (scale may be null: 1)
+template <typename T>
+void qms_launch_pl_from_ref(const QGrid& g, const double* r64, const double* scale, T* out, cudaStream_t st);
+// x[ref] += scale[0] * e[PL]
+template <typename T>
+void qms_launch_ref_add_pl(const QGrid& g, const T* e, const double* scale, double* x, cudaStream_t st);

@@ -16,6 +16,7 @@
 // host; the host only reads the residual estimate to decide when to stop.
 #include "qms_internal.h"
 #include "qms_solver.h"
+#include "qms_pl.h"
 
 #include <cmath>
 #include <cstdio>
@@ -114,15 +115,14 @@ __device__ __forceinline__ void store_partials(double* part, float a, float b) {
     if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = s1;
 }
 
+// r holds the normalised residual (converted from the FP64 residual): rh = r, p = v = e = 0
 template <typename T>
-__global__ void qk_bicg_init(long long n, const double* __restrict__ r64, const double* __restrict__ S,
-                             T* __restrict__ r, T* __restrict__ rh, T* __restrict__ p, T* __restrict__ v,
-                             T* __restrict__ e, double* __restrict__ part) {
-    const double inv = S[S_INVNRM];
+__global__ void qk_bicg_init(long long n, const T* __restrict__ r, T* __restrict__ rh, T* __restrict__ p,
+                             T* __restrict__ v, T* __restrict__ e, double* __restrict__ part) {
     float acc = 0.f;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        T rv = (T)(r64[t] * inv);
-        r[t] = rv; rh[t] = rv; p[t] = T(0); v[t] = T(0); e[t] = T(0);
+        const T rv = r[t];
+        rh[t] = rv; p[t] = T(0); v[t] = T(0); e[t] = T(0);
         acc += (float)(rv * rv);
     }
     store_partials<T>(part, acc, 0.f);
@@ -161,13 +161,12 @@ __global__ void qk_bicg_xr(long long n, const T* __restrict__ y, const T* __rest
     store_partials<T>(part, a0, a1);
 }
 
-// r = D (D^-1 r64) / ||.||  (unscaled residual of the normalised system), e = 0
+// r = D r, the unscaled residual of the normalised system (r holds the normalised scaled
+// residual converted from the FP64 one), e = 0
 template <typename T>
-__global__ void qk_cg_init(long long n, const double* __restrict__ r64, const float* __restrict__ dg,
-                           const double* __restrict__ S, T* __restrict__ r, T* __restrict__ e) {
-    const double inv = S[S_INVNRM];
+__global__ void qk_cg_init(long long n, const float* __restrict__ dg, T* __restrict__ r, T* __restrict__ e) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        r[t] = (T)dg[t] * (T)(r64[t] * inv);
+        r[t] = (T)dg[t] * r[t];
         e[t] = T(0);
     }
 }
@@ -176,8 +175,10 @@ __global__ void qk_cg_init(long long n, const double* __restrict__ r64, const fl
 template <typename T>
 __global__ void qk_jacobi(long long n, long long mask_from, const T* __restrict__ r, const float* __restrict__ dg,
                           T* __restrict__ z) {
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        z[t] = t < mask_from ? r[t] / (T)dg[t] : T(0);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const float d = dg[t];                   // 0 on the padding of the layout
+        z[t] = t < mask_from && d != 0.f ? r[t] / (T)d : T(0);
+    }
 }
 
 // partials of r.z and z.z; optionally p = z (first iteration)
@@ -211,12 +212,6 @@ __global__ void qk_cg_p(long long n, const T* __restrict__ z, T* __restrict__ p,
         p[t] = z[t] + be * p[t];
 }
 
-template <typename T>
-__global__ void qk_ir_update(long long n, const T* __restrict__ e, const double* __restrict__ S, double* __restrict__ x) {
-    const double nr = S[S_NRM];
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        x[t] += nr * (double)e[t];
-}
 
 
 // --------------------------------------------------------------------------
@@ -229,22 +224,42 @@ struct GmPtrs { const void* p[GM_MAXM + 1]; };
 // block partials of V_i . w for i = 0..NV-1 (classical Gram-Schmidt projections).
 // NV is a compile-time count so every load of the unrolled loop is unconditional
 // and independent (memory-level parallelism over all basis vectors).
+// 16-byte packets: the padded layout's length is a multiple of 4 elements and every vector
+// starts on a 256-byte boundary, so the Gram-Schmidt sweeps move whole packets
+template <typename T> struct GmPack;
+template <> struct GmPack<float> {
+    using V = float4;
+    static constexpr int W = 4;
+    static __device__ __forceinline__ float at(const V& v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+};
+template <> struct GmPack<double> {
+    using V = double2;
+    static constexpr int W = 2;
+    static __device__ __forceinline__ double at(const V& v, int q) { return q == 0 ? v.x : v.y; }
+};
+
 template <typename T, int NV>
 __global__ void __launch_bounds__(256) qk_gm_dots(long long n, GmPtrs V, const T* __restrict__ w,
                                                   double* __restrict__ part) {
+    using PK = GmPack<T>;
+    using PV = typename PK::V;
     float acc[NV];
 #pragma unroll
     for (int i = 0; i < NV; i++) acc[i] = 0.f;
-    const T* vp[NV];
+    const PV* vp[NV];
 #pragma unroll
-    for (int i = 0; i < NV; i++) vp[i] = (const T*)V.p[i];
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const float wv = (float)w[t];
-        T vv[NV];
+    for (int i = 0; i < NV; i++) vp[i] = (const PV*)V.p[i];
+    const PV* wp = (const PV*)w;
+    const long long np = n / PK::W;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < np; t += (long long)gridDim.x * blockDim.x) {
+        const PV wv = wp[t];
+        PV vv[NV];
 #pragma unroll
         for (int i = 0; i < NV; i++) vv[i] = __ldg(vp[i] + t);
 #pragma unroll
-        for (int i = 0; i < NV; i++) acc[i] += (float)vv[i] * wv;
+        for (int i = 0; i < NV; i++)
+#pragma unroll
+            for (int q = 0; q < PK::W; q++) acc[i] += (float)(PK::at(vv[i], q) * PK::at(wv, q));
     }
     __shared__ double sh[32];
 #pragma unroll
@@ -265,24 +280,34 @@ __global__ void qk_gm_hcol(const double* __restrict__ part, long long nb, int j,
     }
 }
 
-// w -= sum_i h_ij V_i ; partials of |w|^2   (NV = j + 1, compile-time)
+// w -= sum_i h_ij V_i ; partials of |w|^2   (NV = j + 1, compile-time; 16-byte packets)
 template <typename T, int NV>
 __global__ void __launch_bounds__(256) qk_gm_orth(long long n, int j, int m, GmPtrs V, const double* __restrict__ Hm,
                                                   T* __restrict__ w, double* __restrict__ part) {
+    using PK = GmPack<T>;
+    using PV = typename PK::V;
     T h[NV];
-    const T* vp[NV];
+    const PV* vp[NV];
 #pragma unroll
-    for (int i = 0; i < NV; i++) { h[i] = (T)Hm[i * m + j]; vp[i] = (const T*)V.p[i]; }
+    for (int i = 0; i < NV; i++) { h[i] = (T)Hm[i * m + j]; vp[i] = (const PV*)V.p[i]; }
+    PV* wp = (PV*)w;
+    const long long np = n / PK::W;
     float acc = 0.f;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        T vv[NV];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < np; t += (long long)gridDim.x * blockDim.x) {
+        PV vv[NV];
 #pragma unroll
         for (int i = 0; i < NV; i++) vv[i] = __ldg(vp[i] + t);
-        T wv = w[t];
+        PV wv = wp[t];
+        T* wq = reinterpret_cast<T*>(&wv);
 #pragma unroll
-        for (int i = 0; i < NV; i++) wv -= h[i] * vv[i];
-        w[t] = wv;
-        acc += (float)(wv * wv);
+        for (int q = 0; q < PK::W; q++) {
+            T a = wq[q];
+#pragma unroll
+            for (int i = 0; i < NV; i++) a -= h[i] * PK::at(vv[i], q);
+            wq[q] = a;
+            acc += (float)(a * a);
+        }
+        wp[t] = wv;
     }
     __shared__ double sh[32];
     double s0 = qBlockSum(acc, sh);
@@ -327,13 +352,6 @@ __global__ void qk_gm_scale(long long n, const T* __restrict__ w, T* __restrict_
         vout[t] = w[t] * inv;
 }
 
-// v0 = r64 / ||r64|| and g = (beta, 0, ...)
-template <typename T>
-__global__ void qk_gm_init(long long n, const double* __restrict__ r64, const double* __restrict__ S, T* __restrict__ v0) {
-    const double inv = S[S_INVNRM];
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        v0[t] = (T)(r64[t] * inv);
-}
 
 __global__ void qk_gm_reset(int m, double* __restrict__ Gm) {
     for (int q = threadIdx.x; q < 8 + 3 * m + 1; q += blockDim.x) Gm[q] = 0.0;
@@ -354,26 +372,31 @@ __global__ void qk_gm_solve(int k, int m, const double* __restrict__ Hm, double*
     }
 }
 
-// x += sign * nrm * sum_i y_i Z_i   (FP64 accumulation of the refinement; sign -1 undoes it)
+// x[ref] += nrm * sum_i y_i Z_i[PL]   (FP64 accumulation of the refinement); one thread per
+// node, its (up to) four unknowns
 template <typename T, int NV>
-__global__ void __launch_bounds__(256) qk_gm_update(long long n, int m, GmPtrs Z, const double* __restrict__ Gm,
-                                                    const double* __restrict__ S, double nrm_host, double sign,
-                                                    double* __restrict__ x) {
+__global__ void __launch_bounds__(128) qk_gm_update(QGrid g, int m, GmPtrs Z, const double* __restrict__ Gm,
+                                                    const double* __restrict__ S, double* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > g.Nx) return;
     const double* yv = Gm + 8 + 3 * m + 1;
     T y[NV];
     const T* zp[NV];
 #pragma unroll
-    for (int i = 0; i < NV; i++) { y[i] = (T)yv[i]; zp[i] = (const T*)Z.p[i]; }
-    const double nr = sign * (S ? S[S_NRM] : nrm_host);
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        T zz[NV];
-#pragma unroll
-        for (int i = 0; i < NV; i++) zz[i] = __ldg(zp[i] + t);
+    for (int q = 0; q < NV; q++) { y[q] = (T)yv[q]; zp[q] = (const T*)Z.p[q]; }
+    const double nr = S[S_NRM];
+    const QPL L = qms_pl(g);
+    const long long nd = qms_pl_node(g, L, i, j, k);
+    auto comb = [&](long long t) {
         T acc = T(0);
 #pragma unroll
-        for (int i = 0; i < NV; i++) acc += y[i] * zz[i];
-        x[t] += nr * (double)acc;
-    }
+        for (int q = 0; q < NV; q++) acc += y[q] * __ldg(zp[q] + t);
+        return nr * (double)acc;
+    };
+    if (i <= g.xs) x[qAX(g, i, j, k)] += comb(nd);
+    if (j <= g.ys) x[qAY(g, i, j, k)] += comb(L.comp + nd);
+    if (k <= g.zs) x[qAZ(g, i, j, k)] += comb(2 * L.comp + nd);
+    x[qV(g, i, j, k)] += comb(3 * L.comp + nd);
 }
 
 // compile-time dispatch on the number of basis vectors (1..GM_MAXM)
@@ -398,10 +421,10 @@ static void gm_orth(int nv, int vb, cudaStream_t st, long long n, int j, int m, 
     }
 }
 template <typename T>
-static void gm_update(int nv, int vb, cudaStream_t st, long long n, int m, const GmPtrs& Z, const double* Gm,
-                      const double* S, double nrm, double sign, double* x) {
+static void gm_update(int nv, cudaStream_t st, const QGrid& g, int m, const GmPtrs& Z, const double* Gm,
+                      const double* S, double* x) {
     switch (nv) {
-#define C(N) case N: qk_gm_update<T, N><<<vb, 256, 0, st>>>(n, m, Z, Gm, S, nrm, sign, x); break;
+#define C(N) case N: qk_gm_update<T, N><<<qms_node_grid(g), 128, 0, st>>>(g, m, Z, Gm, S, x); break;
         GM_CASES(C)
 #undef C
     }
@@ -474,15 +497,19 @@ int QmsSolver::init(const qms_desc& d) {
     if (d.xs < 4 || d.ys < 4 || d.zs < 4) { err = "grid must have at least 4 cells per axis"; return QMS_ERR_ARG; }
     if (!(d.dx > 0 && d.dy > 0 && d.dz > 0 && d.dt > 0)) { err = "dx, dy, dz, dt must be positive"; return QMS_ERR_ARG; }
     g = qms_make_grid(d.xs, d.ys, d.zs, d.dx, d.dy, d.dz);
-    // the stencil kernels index rows with 32-bit integers
-    if (g.n >= 0x7fffffffLL) { err = "grid too large: more than 2^31 - 1 unknowns"; return QMS_ERR_ARG; }
+    // the stencil kernels index rows with 32-bit integers (and the padded layout is a little larger)
+    npl = qms_pl(g).n;
+    if (g.n >= 0x7fffffffLL || npl >= 0x7fffffffLL) {
+        err = "grid too large: more than 2^31 - 1 unknowns";
+        return QMS_ERR_ARG;
+    }
     fp64_inner = d.precision == QMS_PREC_FP64;
     trace = std::getenv("QMS_TRACE") != nullptr;
     tsize = fp64_inner ? sizeof(double) : sizeof(float);
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     vec_blocks = (long long)nsm * 8;
-    long long need = (g.n + 255) / 256;
+    long long need = (npl + 255) / 256;
     if (need < vec_blocks) vec_blocks = need;
     nbop = qms_op_num_blocks(g);
     long long npart = std::max(4 * nbop, (long long)(GM_MAXM + 1) * vec_blocks) + 64;
@@ -505,23 +532,43 @@ int QmsSolver::init(const qms_desc& d) {
     CK(cudaMemsetAsync(S, 0, S_COUNT * 8, st));
     CK(cudaMalloc(&status, sizeof(unsigned)));
     CK(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
-    CK(cudaMalloc(&nc32, 6 * g.Nn * 4));
-    CK(cudaMalloc(&nc64, 6 * g.Nn * 8));
-    CK(cudaMalloc(&dg_steady, n * 4));
-    CK(cudaMalloc(&dg_tr, n * 4));
-    for (auto& p : vec) CK(cudaMalloc(&p, n * tsize));
-    use_mg = d.precond == QMS_PRECOND_MG;
-    CK(cudaMalloc(&mgtmp, n * tsize));
+    CK(cudaMalloc(&nc32, 6 * qms_pl(g).comp * 4));
+    CK(cudaMalloc(&nc64, 6 * qms_pl(g).comp * 8));
+    // inner-solver vectors in the padded layout; the padding stays zero
+    auto pl_alloc = [&](void** p, size_t es) -> cudaError_t {
+        cudaError_t e = cudaMalloc(p, npl * es);
+        return e != cudaSuccess ? e : cudaMemsetAsync(*p, 0, npl * es, st);
+    };
+    CK(pl_alloc((void**)&dg_steady, 4));
+    CK(pl_alloc((void**)&dg_tr, 4));
+    for (auto& p : vec) CK(pl_alloc(&p, tsize));
+    // multigrid needs at least two levels (grids of a few cells use the Jacobi / identity fallback)
+    use_mg = d.precond == QMS_PRECOND_MG && QmsMG<float>::levels_for(g, 5) >= 2;
+    CK(pl_alloc((void**)&mgtmp, tsize));
     if (d.krylov == QMS_KRYLOV_GMRES) {
         const int m = std::min(std::max(d.gmres_m, 1), GM_MAXM);
         desc.gmres_m = m;
-        for (int i = 0; i <= m; i++) CK(cudaMalloc(&gmV[i], n * tsize));
-        if (use_mg) for (int i = 0; i < m; i++) CK(cudaMalloc(&gmZ[i], n * tsize));
+        for (int i = 0; i <= m; i++) CK(pl_alloc(&gmV[i], tsize));
+        if (use_mg) for (int i = 0; i < m; i++) CK(pl_alloc(&gmZ[i], tsize));
         CK(cudaMalloc(&gm_H, (size_t)m * (m + 1) * 8));
         CK(cudaMalloc(&gm_scal, (size_t)(8 + 4 * m + 8) * 8));
     }
     CK(cudaMallocHost(&hS, S_COUNT * 8));
     CK(cudaMemsetAsync(x, 0, n * 8, st));
+    // tensor maps of every padded vector that feeds a stencil kernel, and of the coefficients
+    std::vector<const void*> mapped(vec, vec + QMS_NVEC);
+    mapped.push_back(mgtmp);
+    for (int i = 0; i <= GM_MAXM; i++) if (gmV[i]) mapped.push_back(gmV[i]);
+    for (int i = 0; i < GM_MAXM; i++) if (gmZ[i]) mapped.push_back(gmZ[i]);
+    for (const void* p : mapped) {
+        CUtensorMap mp;
+        if (!qms_make_pl_map(&mp, p, g, (int)tsize, 4, PLXY)) { err = "tensor map encoding failed"; return QMS_ERR_CUDA; }
+        tmaps[p] = mp;
+    }
+    if (!qms_make_pl_map(&cmap32, nc32, g, 4, 6, PLCY) || !qms_make_pl_map(&cmap64, nc64, g, 8, 6, PLCY)) {
+        err = "tensor map encoding failed";
+        return QMS_ERR_CUDA;
+    }
     double vac[6] = {1, 1, 1, 0, 0, 0};
     return set_materials(nullptr, vac, 0);
 }
@@ -533,9 +580,9 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
     return ncell + sizeof(QMatTable<double>) + sizeof(QMatTable<float>) + 4 * g.n * 8 + 3 * ncell * 8 +
-           6 * g.Nn * 12 +
-           3 * smax * 8 + (4 * nb + 64) * 8 + 2 * g.n * 4 + (QMS_NVEC + 1) * g.n * ts + 4096 +
-           (d.krylov == QMS_KRYLOV_GMRES ? (size_t)(2 * d.gmres_m + 1) * g.n * ts : 0) +
+           6 * qms_pl(g).comp * 12 +
+           3 * smax * 8 + (4 * nb + 64) * 8 + 2 * qms_pl(g).n * 4 + (QMS_NVEC + 1) * qms_pl(g).n * ts + 4096 +
+           (d.krylov == QMS_KRYLOV_GMRES ? (size_t)(2 * d.gmres_m + 1) * qms_pl(g).n * ts : 0) +
            (d.precond == QMS_PRECOND_MG ? 2 * (ts == 8 ? QmsMG<double>::bytes_for(g, 5, true) : QmsMG<float>::bytes_for(g, 5, true)) : 0) +
            // conductor-region coarse space: node lists (at most every node) and the K x K pseudo-inverse
            (d.precond == QMS_PRECOND_MG ? (size_t)g.Nn * 8 + (size_t)QMS_REGION_MAX * QMS_REGION_MAX * 8 + 64 * 1024 : 0);
@@ -561,8 +608,8 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     qms_launch_node_coef<float>(g, coef32(), nc32, st);
     qms_launch_node_coef<double>(g, coef64(), nc64, st);
     QCoef<float> c32 = coef32();
-    qms_launch_diag(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
-    qms_launch_diag(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
+    qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
+    qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
     CK(cudaGetLastError());
     if (use_mg) {
         const double vshift = desc.mg_vshift;
@@ -623,6 +670,20 @@ void QmsSolver::op(bool adv, int mode, const QStepPar<T>& P, const T* xin, const
 }
 template void QmsSolver::op<float>(bool, int, const QStepPar<float>&, const float*, const float*, float*,
                                    const float*, double*);
+
+const CUtensorMap& QmsSolver::tmap(const void* p) const { return tmaps.at(p); }
+
+template <typename T>
+void QmsSolver::op_pl(bool adv, int mode, const QStepPar<T>& P, const T* xin, T* y, const T* w, double* partials) {
+    const double ncell = (double)g.xs * g.ys * g.zs;
+    OpEv* ev = prof_begin(sizeof(T) == 8 ? 1 : 0, (double)g.n * sizeof(T) * (2 + (w && w != xin ? 1 : 0)) + ncell);
+    qms_launch_op_pl<T>(g, P, tmap(xin), sizeof(T) == 8 ? cmap64 : cmap32, adv, mode, y, w, partials, status, st);
+    nlaunch++;
+    prof_end(ev);
+}
+template void QmsSolver::op_pl<float>(bool, int, const QStepPar<float>&, const float*, float*, const float*, double*);
+template void QmsSolver::op_pl<double>(bool, int, const QStepPar<double>&, const double*, double*, const double*,
+                                       double*);
 template void QmsSolver::op<double>(bool, int, const QStepPar<double>&, const double*, const double*, double*,
                                     const double*, double*);
 
@@ -690,20 +751,23 @@ void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool
     if (use_mg) {
         OpEv* ev = prof_begin(2, 0.0);
         if (sizeof(T) == 4)
-            nlaunch += mgf[transient ? 1 : 0].vcycle((const float*)r, bscale, (float*)z, (float*)mgtmp, mask_v, st);
+            nlaunch += mgf[transient ? 1 : 0].vcycle((const float*)r, bscale != nullptr, (float*)z, tmap(z),
+                                                     (float*)mgtmp, tmap(mgtmp), cmap32, mask_v, status, st);
         else
-            nlaunch += mgd[transient ? 1 : 0].vcycle((const double*)r, bscale, (double*)z, (double*)mgtmp, mask_v, st);
+            nlaunch += mgd[transient ? 1 : 0].vcycle((const double*)r, bscale != nullptr, (double*)z, tmap(z),
+                                                     (double*)mgtmp, tmap(mgtmp), cmap64, mask_v, status, st);
         if (!mask_v) regions.apply<T>(r, bscale, z, st, nlaunch);
         prof_end(ev);
     } else if (jacobi_pcg) {
-        qk_jacobi<T><<<(int)vec_blocks, 256, 0, st>>>(g.n, mask_v ? g.oV : g.n, r, transient ? dg_tr : dg_steady, z);
+        qk_jacobi<T><<<(int)vec_blocks, 256, 0, st>>>(npl, mask_v ? 3 * qms_pl(g).comp : npl, r,
+                                                        transient ? dg_tr : dg_steady, z);
         nlaunch++;
     }
 }
 
 template <typename T>
 int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& iters) {
-    const long long n = g.n;
+    const long long n = npl;
     T* r = (T*)vec[0]; T* rh = (T*)vec[1]; T* p = (T*)vec[2]; T* vv = (T*)vec[3];
     T* s = (T*)vec[4]; T* t = (T*)vec[5]; T* e = (T*)vec[6];
     // right preconditioner of the row-scaled operator D^-1 M: y = MG(D p); identity without MG
@@ -712,8 +776,9 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
     const float* dg = transient ? dg_tr : dg_steady;
     QStepPar<T> P = qms_step_par<T>(g, v[0], v[1], v[2], desc.dt, transient);
     const int vb = (int)vec_blocks;
-    qk_bicg_init<T><<<vb, 256, 0, st>>>(n, r64, S, r, rh, p, vv, e, part);
-    nlaunch++;
+    qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, r, st);
+    qk_bicg_init<T><<<vb, 256, 0, st>>>(n, r, rh, p, vv, e, part);
+    nlaunch += 2;
     finalize(FIN_BICG_INIT, 1, vec_blocks);
     const double tol2 = desc.inner_rtol * desc.inner_rtol;
     iters = 0;
@@ -721,12 +786,12 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
         qk_bicg_p<T><<<vb, 256, 0, st>>>(n, r, p, vv, S);
         nlaunch++;
         if (use_mg) precond<T>(p, dg, y, false, transient, false);
-        op<T>(adv, QOPH_SCALED, P, y, nullptr, vv, rh, part);
+        op_pl<T>(adv, QOPH_SCALED, P, y, vv, rh, part);
         finalize(FIN_BICG_ALPHA, 1, nbop);
         qk_bicg_s<T><<<vb, 256, 0, st>>>(n, r, vv, s, S);
         nlaunch++;
         if (use_mg) precond<T>(s, dg, z, false, transient, false);
-        op<T>(adv, QOPH_SCALED, P, z, nullptr, t, s, part);
+        op_pl<T>(adv, QOPH_SCALED, P, z, t, s, part);
         finalize(FIN_BICG_OMEGA, 2, nbop);
         qk_bicg_xr<T><<<vb, 256, 0, st>>>(n, y, z, s, t, rh, e, r, S, part);
         nlaunch++;
@@ -745,7 +810,7 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
             break;
         }
     }
-    qk_ir_update<T><<<vb, 256, 0, st>>>(n, e, S, x);
+    qms_launch_ref_add_pl<T>(g, e, S + S_NRM, x, st);
     nlaunch++;
     CK(cudaGetLastError());
     return 0;
@@ -754,7 +819,7 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
 
 template <typename T>
 int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& iters, int fixed_k) {
-    const long long n = g.n;
+    const long long n = npl;
     const int m = std::min(desc.gmres_m, GM_MAXM);
     const int kmax = fixed_k > 0 ? std::min(fixed_k, m) : m;
     const float* dg = transient ? dg_tr : dg_steady;
@@ -765,7 +830,7 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
     for (int i = 0; i < m; i++) Zp.p[i] = use_mg ? gmZ[i] : gmV[i];
     T* w = (T*)vec[0];
     qk_gm_reset<<<1, 128, 0, st>>>(m, gm_scal);
-    qk_gm_init<T><<<vb, 256, 0, st>>>(n, r64, S, (T*)gmV[0]);
+    qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, (T*)gmV[0], st);
     nlaunch += 2;
     const double tol = desc.inner_rtol;
     int k = 0;
@@ -773,7 +838,7 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
         T* vj = (T*)gmV[j];
         T* zj = use_mg ? (T*)gmZ[j] : vj;
         if (use_mg) precond<T>(vj, dg, zj, false, transient, false);
-        op<T>(adv, QOPH_SCALED, P, zj, nullptr, w, nullptr, nullptr);
+        op_pl<T>(adv, QOPH_SCALED, P, zj, w, nullptr, nullptr);
         gm_dots<T>(j + 1, vb, st, n, Vp, w, part);
         qk_gm_hcol<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H);
         gm_orth<T>(j + 1, vb, st, n, j, m, Vp, gm_H, w, part);
@@ -788,7 +853,7 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
         }
     }
     qk_gm_solve<<<1, 32, 0, st>>>(k, m, gm_H, gm_scal);
-    gm_update<T>(k, vb, st, n, m, Zp, gm_scal, S, 0.0, 1.0, x);
+    gm_update<T>(k, st, g, m, Zp, gm_scal, S, x);
     nlaunch += 2;
     last_gm_k = k;
     iters = k;
@@ -799,14 +864,15 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
 
 template <typename T>
 int QmsSolver::inner_pcg(bool transient, int& iters) {
-    const long long n = g.n;
+    const long long n = npl;
     T* r = (T*)vec[0]; T* z = (T*)vec[1]; T* p = (T*)vec[2]; T* q = (T*)vec[3]; T* e = (T*)vec[6];
     const float* dg = transient ? dg_tr : dg_steady;
     QStepPar<T> P = qms_step_par<T>(g, 0, 0, 0, desc.dt, transient);
     const int vb = (int)vec_blocks;
     // V block frozen at zero: the steady magnetostatic system with v = 0 has V = 0
-    qk_cg_init<T><<<vb, 256, 0, st>>>(n, r64, dg, S, r, e);
-    nlaunch++;
+    qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, r, st);
+    qk_cg_init<T><<<vb, 256, 0, st>>>(n, dg, r, e);
+    nlaunch += 2;
     precond<T>(r, nullptr, z, true, transient, true);
     qk_cg_dot<T><<<vb, 256, 0, st>>>(n, r, z, p, part);
     nlaunch++;
@@ -814,7 +880,7 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
     const double tol2 = desc.inner_rtol * desc.inner_rtol;
     iters = 0;
     for (int it = 0; it < desc.max_inner; it++) {
-        op<T>(false, QOPH_APPLY, P, p, nullptr, q, p, part);
+        op_pl<T>(false, QOPH_APPLY, P, p, q, p, part);
         finalize(FIN_CG_ALPHA, 1, nbop);
         qk_cg_update<T><<<vb, 256, 0, st>>>(n, p, q, S, e, r);
         nlaunch++;
@@ -831,7 +897,7 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
         qk_cg_p<T><<<vb, 256, 0, st>>>(n, z, p, S);
         nlaunch++;
     }
-    qk_ir_update<T><<<vb, 256, 0, st>>>(n, e, S, x);
+    qms_launch_ref_add_pl<T>(g, e, S + S_NRM, x, st);
     nlaunch++;
     CK(cudaGetLastError());
     return 0;

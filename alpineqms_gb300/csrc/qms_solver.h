@@ -3,9 +3,11 @@
 #include "qms.h"
 #include "qms_internal.h"
 #include "qms_mg.h"
+#include "qms_tma.cuh"
 
 #include <algorithm>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #define QMS_NVEC 9   // r, rh, p, v, s, t, e, y, z  (+ MG level-0 temporary)
@@ -73,6 +75,13 @@ struct QmsSolver {
     int profile_collect(qms_profile* out);
     template <typename T>
     void op(bool adv, int mode, const QStepPar<T>& P, const T* x, const T* b, T* y, const T* w, double* partials);
+    // the inner solver's operator on padded vectors (TMA-staged)
+    template <typename T>
+    void op_pl(bool adv, int mode, const QStepPar<T>& P, const T* x, T* y, const T* w, double* partials);
+    long long npl = 0;                              // padded inner-vector length
+    std::unordered_map<const void*, CUtensorMap> tmaps;   // tensor maps of the padded vectors
+    CUtensorMap cmap32{}, cmap64{};                 // ... and of the node coefficients
+    const CUtensorMap& tmap(const void* p) const;
 
     ~QmsSolver();
     void release();

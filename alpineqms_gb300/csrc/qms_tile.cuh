@@ -6,6 +6,7 @@
 // (planes k-1 and k, with a -1 halo in i and j) are staged in a three-plane ring.
 #pragma once
 #include "qms_common.cuh"
+#include "qms_tma.cuh"
 
 #define OTX 32
 #define OTY 8
@@ -105,7 +106,8 @@ struct CStager {
             const int li = q % (OTX + 1), lj = q / (OTX + 1);
             const int i = i0 - 1 + li, j = j0 - 1 + lj;
             soff[e] = ok ? lj * (OTX + 1) + li : -1;
-            noff[e] = ok && i >= 1 && j >= 1 && i <= g.Nx && j <= g.Ny ? (i - 1) + (j - 1) * g.Nx : -1;
+            // node coefficients are stored in the padded layout ([6][Nz][Ny][P], column i)
+            noff[e] = ok && i >= 1 && j >= 1 && i <= g.Nx && j <= g.Ny ? i + (j - 1) * qms_pl(g).P : -1;
         }
     }
     // plane k of the six coefficients into slot tslot(k): cp.async from the stored node
@@ -115,8 +117,9 @@ struct CStager {
         const int sl = tslot(k);
         if (c.nc) {
             const bool kin = k >= 1 && k <= c.g.Nz;
-            const long long N = c.g.Nn;
-            const long long kb = (long long)(k - 1) * c.g.Nx * c.g.Ny;
+            const QPL L = qms_pl(c.g);
+            const long long N = L.comp;
+            const long long kb = (long long)(k - 1) * c.g.Ny * L.P;
 #pragma unroll
             for (int e = 0; e < 2; e++) {
                 if (soff[e] < 0) continue;
@@ -132,7 +135,8 @@ struct CStager {
                 const int li = soff[e] % (OTX + 1), lj = soff[e] / (OTX + 1);
                 T v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
                 if (noff[e] >= 0 && k >= 1 && k <= c.g.Nz) {
-                    const int i = noff[e] % c.g.Nx + 1, j = noff[e] / c.g.Nx + 1;
+                    const int P = qms_pl(c.g).P;
+                    const int i = noff[e] % P, j = noff[e] / P + 1;
                     v0 = c.imux(i, j, k); v1 = c.imuy(i, j, k); v2 = c.imuz(i, j, k);
                     v3 = c.sgx(i, j, k); v4 = c.sgy(i, j, k); v5 = c.sgz(i, j, k);
                 }

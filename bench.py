@@ -195,6 +195,49 @@ def aggregate_replicas(ms_local, units_local, dist=None, device="cpu"):
     return float(mx.item()), float(sm.item())
 
 
+def edge_current(inp, geom, x):
+    """sigma_edge * dV/dh on every x-, y- and z-edge (sigma_edge the mean of the four cells
+    around the edge): how V enters the A rows.  Used to compare potentials up to the
+    floating constant of isolated conductors."""
+    import numpy as np
+    xs, ys, zs = inp.xs, inp.ys, inp.zs
+    Nx, Ny, Nz = xs + 1, ys + 1, zs + 1
+    oV = 4 * Nx * Ny * Nz - Ny * Nz - Nx * Nz - Nx * Ny - Nx * Ny * Nz
+    V = np.asarray(x[oV:]).reshape((Nx, Ny, Nz), order="F")
+    g = np.asarray(geom).reshape((xs, ys, zs), order="F")
+    table = inp.props_table()
+    lut = {int(r[0]): r[4:7] for r in table}
+    sig = np.zeros((3, xs, ys, zs))
+    for mid, sv in lut.items():
+        m = g == mid
+        for a in range(3):
+            sig[a][m] = sv[a]
+    out = []
+    for a, (d, n) in enumerate(((inp.dx, xs), (inp.dy, ys), (inp.dz, zs))):
+        s = np.pad(sig[a], 1)                   # cells with a zero halo
+        # edge along axis a from node p: the four cells sharing it (other two indices p-1, p)
+        if a == 0:
+            se = 0.25 * (s[1:-1, :-1, :-1] + s[1:-1, 1:, :-1] + s[1:-1, :-1, 1:] + s[1:-1, 1:, 1:])
+            dv = (V[1:] - V[:-1]) / d
+        elif a == 1:
+            se = 0.25 * (s[:-1, 1:-1, :-1] + s[1:, 1:-1, :-1] + s[:-1, 1:-1, 1:] + s[1:, 1:-1, 1:])
+            dv = (V[:, 1:] - V[:, :-1]) / d
+        else:
+            se = 0.25 * (s[:-1, :-1, 1:-1] + s[1:, :-1, 1:-1] + s[:-1, 1:, 1:-1] + s[1:, 1:, 1:-1])
+            dv = (V[:, :, 1:] - V[:, :, :-1]) / d
+        # the reference forms edge conductivities only for node indices 2..size (F:258-269)
+        mask = np.zeros(se.shape, bool)
+        mask[1:xs if a != 0 else xs, 1:ys if a != 1 else ys, 1:zs if a != 2 else zs] = True
+        if a == 0:
+            mask[0] = False
+        elif a == 1:
+            mask[:, 0] = False
+        else:
+            mask[:, :, 0] = False
+        out.append((np.where(mask, se, 0.0) * dv).ravel(order="F"))
+    return np.concatenate(out)
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import numpy as np
@@ -216,8 +259,9 @@ def run_gpu(args):
     kw = {}
     if args.check_every:
         kw["check_every"] = args.check_every
-    solver = QMSSolver(default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt,
-                                    precision=args.precision, device=local, **kw))
+    desc = default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt, precision=args.precision,
+                        device=local, **kw)
+    solver = QMSSolver(desc)
     solver.set_geometry_f64(geom, inp.props_table())
     n = solver.n
     sched = VelocitySchedule(inp.traj, inp.dt)
@@ -301,11 +345,15 @@ def run_gpu(args):
         def rel(a, b):
             nb = float(np.linalg.norm(b))
             return float(np.linalg.norm(a - b)) / nb if nb > 0 else float(np.linalg.norm(a))
+        jm, jd = edge_current(inp, geom, xm), edge_current(inp, geom, xd)
         accuracy = {"vs": "fp64 GPU solver (tol 1e-14), same start state, one step", "step": counter,
-                    "rel_l2_A": rel(xm[:oV], xd[:oV]), "rel_l2_V": rel(xm[oV:], xd[oV:]),
+                    "rel_l2_A": rel(xm[:oV], xd[:oV]), "rel_l2_J": rel(jm, jd),
                     "rel_l2_H": rel(np.concatenate([h.ravel() for h in hm]), np.concatenate([h.ravel() for h in hd])),
+                    "rel_l2_V_raw": rel(xm[oV:], xd[oV:]),
+                    "note": "V enters through sigma grad V (J); an isolated conductor's potential carries an "
+                            "arbitrary constant that no residual sees",
                     "fp64_iters": {"outer": st64["outer"], "inner": st64["inner"]}}
-        accuracy["pass_1e-8"] = all(accuracy[k] <= 1e-8 for k in ("rel_l2_A", "rel_l2_V", "rel_l2_H"))
+        accuracy["pass_1e-8"] = all(accuracy[k] <= 1e-8 for k in ("rel_l2_A", "rel_l2_J", "rel_l2_H"))
         s64.close()
 
     peak, peak_kind = measured_peak()
@@ -338,7 +386,7 @@ def run_gpu(args):
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
                 "config": {"workload": "moving_plate_256", "grid": [inp.xs, inp.ys, inp.zs], "dof": n,
-                           "dt": inp.dt, "precision": args.precision, "tol": 1e-12,
+                           "dt": inp.dt, "precision": args.precision, "tol": desc.tol,
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                            "l2": "inputs larger than L2 (one FP32 vector = %.0f MB)" % (n * 4 / 1e6)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": prof["launches"],

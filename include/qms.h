@@ -67,7 +67,8 @@ enum {
     QMS_STATUS_BAD_MATERIAL = 1,
     QMS_STATUS_NAN = 2,
     QMS_STATUS_NO_CONVERGENCE = 4,
-    QMS_STATUS_BREAKDOWN = 8
+    QMS_STATUS_BREAKDOWN = 8,
+    QMS_STATUS_TIMEOUT = 16      /* a bounded device-side wait for a tile copy gave up */
 };
 
 typedef struct {
