@@ -662,7 +662,8 @@ template <typename T>
 void QmsSolver::op(bool adv, int mode, const QStepPar<T>& P, const T* xin, const T* bin, T* y, const T* w,
                    double* partials) {
     const double ncell = (double)g.xs * g.ys * g.zs;
-    OpEv* ev = prof_begin(sizeof(T) == 8 ? 1 : 0,
+    // the reference-layout operator serves the FP64 refinement residual (profile kind 3)
+    OpEv* ev = prof_begin(mode == QOPH_RESID ? 3 : (sizeof(T) == 8 ? 1 : 0),
                           (double)g.n * sizeof(T) * (2 + (w && w != xin ? 1 : 0) + (bin ? 1 : 0)) + ncell);
     qms_launch_operator<T>(g, coef<T>(), P, adv, mode, xin, bin, y, w, partials, st);
     nlaunch++;
@@ -715,6 +716,7 @@ bool QmsSolver::prof_accum(const OpEv& e) {
     }
     if (e.kind == 1) { profacc.op64_launches++; profacc.op64_ms += ms; profacc.op64_bytes += e.bytes; }
     else if (e.kind == 0) { profacc.op32_launches++; profacc.op32_ms += ms; profacc.op32_bytes += e.bytes; }
+    else if (e.kind == 3) { profacc.resid_launches++; profacc.resid_ms += ms; profacc.resid_bytes += e.bytes; }
     else { profacc.mg_cycles++; profacc.mg_ms += ms; }
     return true;
 }

@@ -60,7 +60,7 @@ struct QmsSolver {
     // instrumentation (qms_profile_enable)
     bool prof = false;
     long long nlaunch = 0;
-    struct OpEv { cudaEvent_t a, b; int kind; double bytes; };   // kind: 0 op32, 1 op64, 2 V-cycle
+    struct OpEv { cudaEvent_t a, b; int kind; double bytes; };   // kind: 0 op32, 1 op64, 2 V-cycle, 3 FP64 residual
     OpEv* prof_begin(int kind, double bytes);
     void prof_end(OpEv* ev);
     bool prof_accum(const OpEv& e);              // false when the events cannot be timed

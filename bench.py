@@ -357,21 +357,31 @@ def run_gpu(args):
         s64.close()
 
     peak, peak_kind = measured_peak()
-    kern = "qk_operator_f32" if prof["op32_ms"] >= prof["op64_ms"] else "qk_operator_f64_resid"
-    kms = prof["op32_ms"] if kern == "qk_operator_f32" else prof["op64_ms"]
-    kbytes = prof["op32_bytes"] if kern == "qk_operator_f32" else prof["op64_bytes"]
-    klaunch = prof["op32_launches"] if kern == "qk_operator_f32" else prof["op64_launches"]
+    # The roofline kernel is the inner solver's stencil (the TMA-staged operator on the padded
+    # layout): algorithmic bytes 2 p n + cells per launch (x and y, one material byte per cell).
+    inner = "fp32" if args.precision == "mixed" else "fp64"
+    kms = prof["op32_ms"] if inner == "fp32" else prof["op64_ms"]
+    kbytes = prof["op32_bytes"] if inner == "fp32" else prof["op64_bytes"]
+    klaunch = prof["op32_launches"] if inner == "fp32" else prof["op64_launches"]
+    kern = "qk_op_pl<float> (inner stencil, TMA)" if inner == "fp32" else "qk_op_pl<double> (inner stencil, TMA)"
     achieved = kbytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
-    tr = ncu_traffic(kern)
+    tr = ncu_traffic("qk_op_pl_f32" if inner == "fp32" else "qk_op_pl_f64")
     roofline = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6800 GB/s",
                 "traffic": (tr * n if tr else None), "launches": klaunch,
                 "avg_launch_us": 1e3 * kms / max(klaunch, 1),
                 "algorithmic_bytes_per_launch": kbytes / max(klaunch, 1),
+                "algorithmic_bytes_def": "2 p n_dims + cells (x, y, one material byte per cell)",
                 "share_of_step": kms / ms if ms > 0 else None,
                 "op32_ms": prof["op32_ms"], "op64_ms": prof["op64_ms"], "mg_ms": prof["mg_ms"],
                 "mg_cycles": prof["mg_cycles"]}
+    if prof["resid_launches"] > 0:
+        # the FP64 refinement residual is bound by GB300's FP64 rate, not by HBM
+        roofline["fp64_residual"] = {"launches": prof["resid_launches"], "ms": prof["resid_ms"],
+                                     "avg_launch_us": 1e3 * prof["resid_ms"] / prof["resid_launches"],
+                                     "achieved_gbs": prof["resid_bytes"] / (prof["resid_ms"] / 1e3) / 1e9
+                                     if prof["resid_ms"] > 0 else None}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -162,14 +162,17 @@ int qms_residual_norm(qms_handle* h, int transient, const double v[3], double* r
  * the handle is counted.  Enabling resets the counters. */
 typedef struct {
     int64_t launches;        /* all kernel launches since the reset */
-    int64_t op32_launches;   /* FP32 operator applications */
+    int64_t op32_launches;   /* FP32 inner operator applications */
     double op32_ms;          /* their summed device time */
     double op32_bytes;       /* their summed algorithmic bytes (x, y, dot vector, material slots) */
-    int64_t op64_launches;   /* FP64 operator applications (residuals) */
+    int64_t op64_launches;   /* FP64 inner operator applications (QMS_PREC_FP64) */
     double op64_ms;
     double op64_bytes;
     int64_t mg_cycles;       /* multigrid V-cycles */
     double mg_ms;            /* their summed device time */
+    int64_t resid_launches;  /* FP64 refinement residuals r = D^-1 (b - M x) */
+    double resid_ms;
+    double resid_bytes;
 } qms_profile;
 int qms_profile_enable(qms_handle* h, int on);
 int qms_get_profile(qms_handle* h, qms_profile* out);
