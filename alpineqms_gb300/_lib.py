@@ -38,7 +38,8 @@ class QmsDesc(ctypes.Structure):
                 ("mg_vshift", ctypes.c_double),
                 ("krylov", ctypes.c_int),
                 ("gmres_m", ctypes.c_int),
-                ("use_graphs", ctypes.c_int), ("mg_region_cut", ctypes.c_double)]
+                ("use_graphs", ctypes.c_int), ("mg_region_cut", ctypes.c_double),
+                ("mg_alpha", ctypes.c_double), ("mg_coupling", ctypes.c_int)]
 
 
 class QmsStats(ctypes.Structure):

@@ -49,6 +49,8 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->gmres_m = 32;
     d->use_graphs = 1;
     d->mg_region_cut = 0.0;
+    d->mg_alpha = 1.5;
+    d->mg_coupling = 1;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }
@@ -64,6 +66,7 @@ int qms_create(const qms_desc* d, qms_handle** out) {
     if (!h) return QMS_ERR_NOMEM;
     qms_desc dd = *d;
     if (dd.check_every <= 0) dd.check_every = 1;
+    if (!(dd.mg_alpha > 0)) dd.mg_alpha = 1.0;
     if (dd.max_inner <= 0 || dd.max_outer < 0 || !(dd.tol > 0) || !(dd.inner_rtol > 0) || dd.mg_sweeps < 1 ||
         !(dd.mg_omega > 0)) {
         std::lock_guard<std::mutex> lk(g_err_mu);

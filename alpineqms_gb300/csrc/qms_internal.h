@@ -4,7 +4,9 @@
 
 struct QmsExcite { double B[3]; double G[9]; double v[3]; };
 
-enum QOpModeH { QOPH_APPLY = 0, QOPH_SCALED = 1, QOPH_RESID = 2 };
+// QOPH_VCOUPLE (padded-layout stencil only): y_V = w_V - D_V^-1 (M_VA x_A) on the V rows, the
+// A-to-V coupling of the operator applied to x's A blocks (x's V block is not read)
+enum QOpModeH { QOPH_APPLY = 0, QOPH_SCALED = 1, QOPH_RESID = 2, QOPH_VCOUPLE = 3 };
 
 // qms_exact.cu
 long long qms_launch_assemble(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const QmsExcite& ex,

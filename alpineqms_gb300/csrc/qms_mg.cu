@@ -307,17 +307,28 @@ __device__ __forceinline__ T mg_rcp(T d) {
     else return T(1) / d;
 }
 
-template <typename T, int KIND>
+// QS selects the blocks a cycle works on: 0 all four, 1 the three A blocks, 2 the V block
+// (then only the three conductivities are staged).  xmap / cmap cover exactly those blocks /
+// arrays; b, xout and the rows stay those of the whole padded vector, bc that of the level-1
+// view of the same blocks.
+template <int QS> struct MG0Set {
+    static constexpr int NQ = QS == 0 ? 4 : (QS == 1 ? 3 : 1), Q0 = QS == 2 ? 3 : 0;
+    static constexpr int NC = QS == 2 ? 3 : 6, C0 = QS == 2 ? 3 : 0;
+    static constexpr bool A = QS != 2, V = QS != 1;
+};
+
+template <typename T, int KIND, int QS>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __restrict__ b, int scaled,
           const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap, T* __restrict__ xout,
           MGLevelDev<T> C, T* __restrict__ bc, unsigned* __restrict__ err) {
-    using TL = PLTiles<T>;
+    using S = MG0Set<QS>;
+    using TL = PLTiles<T, S::NQ, S::NC>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][4][PLXY][PLX]
-    T* csm = xsm + 4 * TL::XSLOT;                             // [3 slots][6][PLCY][PLX]
+    T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][NQ][PLXY][PLX]
+    T* csm = xsm + 4 * TL::XSLOT;                             // [3 slots][NC][PLCY][PLX]
     __shared__ __align__(8) uint64_t xbar[4], cbar[3];
-    __shared__ T red[KIND == 2 ? 4 : 1][OTY][OTX];
+    __shared__ T red[KIND == 2 ? S::NQ : 1][OTY][OTX];
     constexpr bool STAGE = KIND != 0;
     const int tid = threadIdx.x + OTX * threadIdx.y;
     const int i0 = blockIdx.x * OTX + 1, j0 = blockIdx.y * OTY + 1, k0 = blockIdx.z * OKB + 1;
@@ -372,10 +383,12 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
     // (1 + vshift on V, 1 on A): it is formed from the staged coefficients, not read.
     T bn0 = T(0), bn1 = T(0), bn2 = T(0), bn3 = T(0);
     auto fetch_b = [&](int kk, long long n) {
-        bn0 = exX ? __ldg(b + n) : T(0);
-        bn1 = exY ? __ldg(b + L.comp + n) : T(0);
-        bn2 = inij && kk <= g.zs ? __ldg(b + 2 * L.comp + n) : T(0);
-        bn3 = inij && !mask_v ? __ldg(b + 3 * L.comp + n) : T(0);
+        if (S::A) {
+            bn0 = exX ? __ldg(b + n) : T(0);
+            bn1 = exY ? __ldg(b + L.comp + n) : T(0);
+            bn2 = inij && kk <= g.zs ? __ldg(b + 2 * L.comp + n) : T(0);
+        }
+        if (S::V) bn3 = inij && !mask_v ? __ldg(b + 3 * L.comp + n) : T(0);
     };
     fetch_b(k0, nd);
     for (int k = k0; k <= kend; k++) {
@@ -396,8 +409,8 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
         const T* ccur = csm + (k % 3) * TL::CSLOT;
         const bool kfA = k <= 2 || k >= g.Nz - 1;       // k terms of qFixX / qFixY / qFixV
         const bool kfZ = k == 1 || k == g.zs;           // k term of qFixZ
-#define CF(q, dk, dj, di) (dk < 0 ? cprv : ccur)[((q) * PLCY + lj + (dj)) * PLX + li + (di)]
-#define XS(q, sl, dj, di) (sl)[((q) * PLXY + lj + (dj)) * PLX + li + (di)]
+#define CF(q, dk, dj, di) (dk < 0 ? cprv : ccur)[((q) - S::C0) * PLCY * PLX + (lj + (dj)) * PLX + li + (di)]
+#define XS(q, sl, dj, di) (sl)[((q) - S::Q0) * PLXY * PLX + (lj + (dj)) * PLX + li + (di)]
         T r[4] = {T(0), T(0), T(0), T(0)};
         // one component: links (wxp, wxm, wyp, wym, wzp, wzm), extra diagonal
         auto point = [&](int q, bool exists, bool fixed, long long row, T bq, T wxp, T wxm, T wyp, T wym, T wzp,
@@ -419,9 +432,10 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
             const T Ax = wxp * (xc - XS(q, x0, 0, 1)) + wxm * (xc - XS(q, x0, 0, -1)) + wyp * (xc - XS(q, x0, 1, 0)) +
                          wym * (xc - XS(q, x0, -1, 0)) + wzp * (xc - XS(q, xp, 0, 0)) + wzm * (xc - XS(q, xm, 0, 0)) +
                          (dextra * dscale + (wxp + wxm + wyp + wym + wzp + wzm) * (dscale - T(1))) * xc;
-            if (KIND == 2) r[q] = bv - Ax;
+            if (KIND == 2) r[q - S::Q0] = bv - Ax;
             else xout[row] = xc + omega * (bv - Ax) * mg_rcp(d);
         };
+        if constexpr (S::A) {
         point(0, exX, fijX || kfA, nd, b0,
               CF(0, 0, 0, 0) * P.idx2, CF(0, 0, 0, -1) * P.idx2, CF(2, 0, 0, 0) * P.idy2,
               CF(2, 0, -1, 0) * P.idy2, CF(1, 0, 0, 0) * P.idz2, CF(1, -1, 0, 0) * P.idz2,
@@ -434,7 +448,8 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
               CF(1, 0, 0, 0) * P.idx2, CF(1, 0, 0, -1) * P.idx2, CF(0, 0, 0, 0) * P.idy2,
               CF(0, 0, -1, 0) * P.idy2, CF(2, 0, 0, 0) * P.idz2, CF(2, -1, 0, 0) * P.idz2,
               CF(5, 0, 0, 0) * P.idt, T(1), T(1));
-        {
+        }
+        if constexpr (S::V) {
             const T fl = P.sigfloor;
             point(3, inij, fijV || kfA, 3 * L.comp + nd, b3,
                   fmax(CF(3, 0, 0, 0), fl) * P.idx2, fmax(CF(3, 0, 0, -1), fl) * P.idx2,
@@ -446,7 +461,7 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
         nd += plane;
         if (KIND == 2) {
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
+            for (int q = 0; q < S::NQ; q++) {
                 r[q] += __shfl_xor_sync(0xffffffffu, r[q], 1);            // i pairs (2p+1, 2p+2)
                 red[q][threadIdx.y][threadIdx.x] = r[q];
             }
@@ -454,18 +469,18 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
             if (!(threadIdx.x & 1) && !(threadIdx.y & 1)) {
                 const bool first = ((k - k0) & 1) == 0;                    // k pairs (odd, even)
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < S::NQ; q++) {
                     const T v = red[q][threadIdx.y][threadIdx.x] + red[q][threadIdx.y + 1][threadIdx.x];
                     acc[q] = first ? v : acc[q] + v;
                 }
                 if (!first || k == kend) {
                     const int I = (i - 1) >> 1, J = (j - 1) >> 1, K = (k - 1) >> 1;
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
+                    for (int q = 0; q < S::NQ; q++) {
                         const MGBlockDesc& cb = C.blk[q];
                         if (I < cb.n1 && J < cb.n2 && K < cb.n3)
                             bc[cb.off + I + (long long)J * cb.n1 + (long long)K * cb.n1 * cb.n2] =
-                                (mask_v && q == 3) ? T(0) : acc[q];
+                                (mask_v && q + S::Q0 == 3) ? T(0) : acc[q];
                     }
                 }
             }
@@ -476,27 +491,31 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
 // level 0: x += alpha P x_c on the active points (the Dirichlet points of every component,
 // and V when masked, stay zero); one thread per node (i, j, k), its (up to) four unknowns
 // in the padded layout
-template <typename T>
+// (C and xc: the level-1 view of the blocks of QS)
+template <typename T, int QS>
 __global__ void mg0_prolong(QGrid g, int mask_v, T* __restrict__ x, MGLevelDev<T> C, const T* __restrict__ xc,
                             T alpha) {
+    using S = MG0Set<QS>;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
     if (i > g.Nx) return;
     const int I = (i - 1) >> 1, J = (j - 1) >> 1, K = (k - 1) >> 1;
     auto coarse = [&](int q) {
-        const MGBlockDesc& cb = C.blk[q];
+        const MGBlockDesc& cb = C.blk[q - S::Q0];
         return xc[cb.off + I + (long long)J * cb.n1 + (long long)K * cb.n1 * cb.n2];
     };
     const QPL L = qms_pl(g);
     const long long nd = qms_pl_node(g, L, i, j, k);
-    if (i <= g.xs && !qFixX(g, i, j, k)) x[nd] += alpha * coarse(0);
-    if (j <= g.ys && !qFixY(g, i, j, k)) x[L.comp + nd] += alpha * coarse(1);
-    if (k <= g.zs && !qFixZ(g, i, j, k)) x[2 * L.comp + nd] += alpha * coarse(2);
-    if (!mask_v && !qFixV(g, i, j, k)) x[3 * L.comp + nd] += alpha * coarse(3);
+    if (S::A) {
+        if (i <= g.xs && !qFixX(g, i, j, k)) x[nd] += alpha * coarse(0);
+        if (j <= g.ys && !qFixY(g, i, j, k)) x[L.comp + nd] += alpha * coarse(1);
+        if (k <= g.zs && !qFixZ(g, i, j, k)) x[2 * L.comp + nd] += alpha * coarse(2);
+    }
+    if (S::V && !mask_v && !qFixV(g, i, j, k)) x[3 * L.comp + nd] += alpha * coarse(3);
 }
 
-template <typename T, int KIND>
+template <typename T, int KIND, int QS = 0>
 static size_t mg0_smem() {
-    return PLTiles<T>::SMEM;
+    return PLTiles<T, MG0Set<QS>::NQ, MG0Set<QS>::NC>::SMEM;
 }
 
 // raise the dynamic shared-memory limit of the level-0 kernels once per device
@@ -507,9 +526,12 @@ static void mg0_prepare() {
     cudaGetDevice(&dev);
     const unsigned long long bit = 1ull << (dev & 63);
     if (done.load(std::memory_order_acquire) & bit) return;
-    cudaFuncSetAttribute(mg0_tiled<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, 0>());
-    cudaFuncSetAttribute(mg0_tiled<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, 1>());
-    cudaFuncSetAttribute(mg0_tiled<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, 2>());
+#define ATTR(K, Q) \
+    cudaFuncSetAttribute(mg0_tiled<T, K, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, K, Q>())
+    ATTR(0, 0); ATTR(1, 0); ATTR(2, 0);
+    ATTR(0, 1); ATTR(1, 1); ATTR(2, 1);
+    ATTR(0, 2); ATTR(1, 2); ATTR(2, 2);
+#undef ATTR
     done.fetch_or(bit, std::memory_order_acq_rel);
 }
 
@@ -581,6 +603,8 @@ void QmsMG<T>::release() {
         for (T* p : ps) if (p) cudaFree(p);
     }
     lv.clear();
+    views[1].clear();
+    views[2].clear();
     if (dminv) cudaFree(dminv);
     if (dmoff) cudaFree(dmoff);
     dminv = nullptr; dmoff = nullptr;
@@ -761,6 +785,24 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
     CKM(cudaMemcpyAsync(dminv, minv.data(), mtot * 8, cudaMemcpyHostToDevice, st));
     CKM(cudaMemcpyAsync(dmoff, moff.data(), C.nb * sizeof(long long), cudaMemcpyHostToDevice, st));
     CKM(cudaStreamSynchronize(st));
+    // views of the three A blocks and of the V block, for cycles on one side of the A-V
+    // coupling: same arrays, block table and pointers restricted to those blocks
+    views[1].assign(lv.begin(), lv.end());
+    views[2].assign(lv.begin(), lv.end());
+    for (size_t l = 0; l < lv.size(); l++) {
+        const long long o = lv[l].blk[3].off;
+        MGLevelDev<T>& A = views[1][l];
+        A.nb = 3;
+        A.total = o;
+        MGLevelDev<T>& V = views[2][l];
+        V.nb = 1;
+        V.blk[0] = lv[l].blk[3];
+        V.blk[0].off = 0;
+        V.total = lv[l].total - o;
+        T** ps[] = {&V.w1, &V.w2, &V.w3, &V.dg, &V.dinv, &V.x, &V.b, &V.t};
+        for (T** q : ps)
+            if (*q) *q += o;
+    }
     return 0;
 }
 
@@ -768,17 +810,29 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
 // result in x0; t0 is a level-0 temporary.  Returns the number of kernel launches.
 template <typename T>
 int QmsMG<T>::vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
-                     const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st) {
+                     const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st, int qs) {
+    if (qs == 1) return vcycle_q<1>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st);
+    if (qs == 2) return vcycle_q<2>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st);
+    return vcycle_q<0>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st);
+}
+
+template <typename T>
+template <int QS>
+int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
+                       const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st) {
     int launches = 0;
+    std::vector<MGLevelDev<T>>& lv = QS == 0 ? this->lv : views[QS];   // levels >= 1 of the cycle's blocks
+    const long long* dmo = dmoff + (QS == 2 ? 3 : 0);                    // their dense coarsest inverses
     const int nl = (int)lv.size();
-    const int mv = mask_v ? 1 : 0;
+    const int mv = (QS == 0 && mask_v) ? 1 : 0;
     const int sc = scaled ? 1 : 0;
     mg0_prepare<T>();
     struct Buf { T* p; const CUtensorMap* m; };
     // level-0 sweeps: KIND 0 writes XO from b; KIND 1 reads XI (tile copies) and writes XO;
     // KIND 2 reads XI and writes the level-1 right-hand side
 #define MG0(KIND, XI, XO, BC)                                                                                     \
-    mg0_tiled<T, KIND><<<g0grid, g0block, mg0_smem<T, KIND>(), st>>>(g0, P0, vshift0, omega, mv, b0, sc, *(XI).m, \
+    mg0_tiled<T, KIND, QS><<<g0grid, g0block, mg0_smem<T, KIND, QS>(), st>>>(g0, P0, vshift0, omega, mv, b0, sc,  \
+                                                                              *(XI).m, \
                                                                        cmap, (XO), lv[1], (BC), err)
     // level 0: nu1 + nu2 sweeps alternate between x0 and t0 (the prolongation is in place);
     // start in t0 when that count is even so that the last write lands in x0
@@ -796,7 +850,7 @@ int QmsMG<T>::vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, 
     for (int l = 1; l < nl; l++) {
         MGLevelDev<T>& L = lv[l];
         if (l == nl - 1) {
-            mg_dense<<<L.nb, 256, 0, st>>>(L, dminv, dmoff, L.b, L.x, mv);
+            mg_dense<<<L.nb, 256, 0, st>>>(L, dminv, dmo, L.b, L.x, mv);
             launches++;
             break;
         }
@@ -828,7 +882,7 @@ int QmsMG<T>::vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, 
         L.x = xl;
         L.t = tl;
     }
-    mg0_prolong<T><<<dim3((g0.Nx + 127) / 128, g0.Ny, g0.Nz), 128, 0, st>>>(g0, mv, x.p, lv[1], lv[1].x, alpha);
+    mg0_prolong<T, QS><<<dim3((g0.Nx + 127) / 128, g0.Ny, g0.Nz), 128, 0, st>>>(g0, mv, x.p, lv[1], lv[1].x, alpha);
     launches++;
     for (int s = 0; s < nu2; s++) {
         MG0(1, x, t.p, nullptr);

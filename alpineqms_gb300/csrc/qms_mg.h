@@ -33,6 +33,7 @@ struct MGLevelDev {
 template <typename T>
 struct QmsMG {
     std::vector<MGLevelDev<T>> lv;
+    std::vector<MGLevelDev<T>> views[3];   // [1]: the A blocks of every level, [2]: the V block
     double* dminv = nullptr;       // dense FP64 inverses of the coarsest blocks
     long long* dmoff = nullptr;
     int nu1 = 2, nu2 = 2;
@@ -57,8 +58,13 @@ struct QmsMG {
     int build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T vshift, cudaStream_t st);
     // z = MG(r) on the padded layout: b0 (scaled by the operator diagonal when `scaled`), x0 the
     // result, t0 a temporary; the tensor maps of x0, t0 and of the node coefficients
+    // qs: 0 all blocks, 1 the A blocks only, 2 the V block only (x0map / t0map then cover those
+    // blocks, cmap the node coefficients they read: all six, or the three conductivities)
     int vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
-               const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st);
+               const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st, int qs = 0);
+    template <int QS>
+    int vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
+                 const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st);
     static int levels_for(const QGrid& g, int min_coarse);
 };
 

@@ -61,8 +61,9 @@ __device__ __forceinline__ T pl_div(T a, T d) {
     else return a / d;
 }
 
-// MODE: QOPH_APPLY (y = M x) or QOPH_SCALED (y = D^-1 M x); partials (optional, FP64):
-// [0] += y . w (w may be null), [1] += y . y
+// MODE: QOPH_APPLY (y = M x), QOPH_SCALED (y = D^-1 M x) or QOPH_VCOUPLE (V rows only:
+// y = w - D^-1 M (x_A, 0)); partials (optional, FP64, not with VCOUPLE): [0] += y . w (w may
+// be null), [1] += y . y
 template <typename T, bool ADV, int MODE>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap,
@@ -116,7 +117,11 @@ qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const
     // FP64 arithmetic per row would make the kernel FP64-throughput bound), FP64 across warps
     using RT = float;
     RT red0 = 0, red1 = 0;
-    auto emit = [&](long long row, T acc, T diag, bool, T) {
+    auto emit = [&](long long row, T acc, T diag, bool is_a, T) {
+        if (MODE == QOPH_VCOUPLE) {           // the A rows are not wanted (dead code)
+            if (!is_a) y[row] = w[row] - pl_div(acc, diag);
+            return;
+        }
         const T out = MODE == QOPH_APPLY ? acc : pl_div(acc, diag);
         y[row] = out;
         if (partials) {
@@ -141,6 +146,7 @@ qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const
         const T* ccur = csm + (k % 3) * TL::CSLOT;
         if (inij) {
             auto xsf = [&](int comp, int dk, int dj, int di) -> T {
+                if (MODE == QOPH_VCOUPLE && comp == 3) return T(0);
                 const T* b = dk < 0 ? xm : (dk > 0 ? xp : x0);
                 return b[(comp * PLXY + lj + dj) * PLX + li + di];
             };
@@ -247,6 +253,8 @@ static void op_pl_prepare() {
     cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
     cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
     cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
     done.fetch_or(bit, std::memory_order_acq_rel);
 }
 
@@ -263,9 +271,11 @@ void qms_launch_op_pl(const QGrid& g, const QStepPar<T>& P, const CUtensorMap& x
 #define L(ADV, MODE) qk_op_pl<T, ADV, MODE><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err)
     if (adv) {
         if (mode == QOPH_APPLY) L(true, QOPH_APPLY);
+        else if (mode == QOPH_VCOUPLE) L(true, QOPH_VCOUPLE);
         else L(true, QOPH_SCALED);
     } else {
         if (mode == QOPH_APPLY) L(false, QOPH_APPLY);
+        else if (mode == QOPH_VCOUPLE) L(false, QOPH_VCOUPLE);
         else L(false, QOPH_SCALED);
     }
 #undef L

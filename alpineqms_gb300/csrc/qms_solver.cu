@@ -474,18 +474,17 @@ void QmsSolver::release() {
     if (gm_H) cudaFree(gm_H);
     if (gm_scal) cudaFree(gm_scal);
     gm_H = gm_scal = nullptr;
-    void* ptrs[] = {ids, dtab64, dtab32, x, b, r64, xbest, H, slicebuf, part, S, status, dg_steady, dg_tr, mgtmp, nc32, nc64};
+    void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,
+                    S,     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
-    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    drop_graphs();
     for (auto& e : evpool) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     evpool.clear();
-    for (auto& e : graph_ev) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
-    graph_ev.clear();
     if (st && own_stream) cudaStreamDestroy(st);
     ids = nullptr; dtab64 = nullptr; dtab32 = nullptr; x = b = r64 = H = slicebuf = part = S = nullptr;
-    status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; xbest = nullptr;
+    status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; mgtmp2 = nullptr; xbest = nullptr;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -545,6 +544,7 @@ int QmsSolver::init(const qms_desc& d) {
     // multigrid needs at least two levels (grids of a few cells use the Jacobi / identity fallback)
     use_mg = d.precond == QMS_PRECOND_MG && QmsMG<float>::levels_for(g, 5) >= 2;
     CK(pl_alloc((void**)&mgtmp, tsize));
+    if (use_mg) CK(pl_alloc((void**)&mgtmp2, tsize));
     if (d.krylov == QMS_KRYLOV_GMRES) {
         const int m = std::min(std::max(d.gmres_m, 1), GM_MAXM);
         desc.gmres_m = m;
@@ -560,12 +560,22 @@ int QmsSolver::init(const qms_desc& d) {
     mapped.push_back(mgtmp);
     for (int i = 0; i <= GM_MAXM; i++) if (gmV[i]) mapped.push_back(gmV[i]);
     for (int i = 0; i < GM_MAXM; i++) if (gmZ[i]) mapped.push_back(gmZ[i]);
+    if (mgtmp2) mapped.push_back(mgtmp2);
+    const long long vbytes = 3 * qms_pl(g).comp * (long long)tsize;   // offset of the V block
     for (const void* p : mapped) {
-        CUtensorMap mp;
-        if (!qms_make_pl_map(&mp, p, g, (int)tsize, 4, PLXY)) { err = "tensor map encoding failed"; return QMS_ERR_CUDA; }
+        CUtensorMap mp, ma, mv;
+        if (!qms_make_pl_map(&mp, p, g, (int)tsize, 4, PLXY) || !qms_make_pl_map(&ma, p, g, (int)tsize, 3, PLXY) ||
+            !qms_make_pl_map(&mv, (const char*)p + vbytes, g, (int)tsize, 1, PLXY)) {
+            err = "tensor map encoding failed";
+            return QMS_ERR_CUDA;
+        }
         tmaps[p] = mp;
+        tmapsA[p] = ma;
+        tmapsV[p] = mv;
     }
-    if (!qms_make_pl_map(&cmap32, nc32, g, 4, 6, PLCY) || !qms_make_pl_map(&cmap64, nc64, g, 8, 6, PLCY)) {
+    const long long cv = 3 * qms_pl(g).comp;                          // first conductivity array
+    if (!qms_make_pl_map(&cmap32, nc32, g, 4, 6, PLCY) || !qms_make_pl_map(&cmap64, nc64, g, 8, 6, PLCY) ||
+        !qms_make_pl_map(&cmapV32, nc32 + cv, g, 4, 3, PLCY) || !qms_make_pl_map(&cmapV64, nc64 + cv, g, 8, 3, PLCY)) {
         err = "tensor map encoding failed";
         return QMS_ERR_CUDA;
     }
@@ -576,10 +586,12 @@ int QmsSolver::init(const qms_desc& d) {
 size_t qms_device_bytes_impl(const qms_desc& d) {
     QGrid g = qms_make_grid(d.xs, d.ys, d.zs, d.dx, d.dy, d.dz);
     size_t ts = d.precision == QMS_PREC_FP64 ? 8 : 4;
+    // the block-triangular preconditioner's V right-hand side
+    size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
-    return ncell + sizeof(QMatTable<double>) + sizeof(QMatTable<float>) + 4 * g.n * 8 + 3 * ncell * 8 +
+    return tri + ncell + sizeof(QMatTable<double>) + sizeof(QMatTable<float>) + 4 * g.n * 8 + 3 * ncell * 8 +
            6 * qms_pl(g).comp * 12 +
            3 * smax * 8 + (4 * nb + 64) * 8 + 2 * qms_pl(g).n * 4 + (QMS_NVEC + 1) * qms_pl(g).n * ts + 4096 +
            (d.krylov == QMS_KRYLOV_GMRES ? (size_t)(2 * d.gmres_m + 1) * qms_pl(g).n * ts : 0) +
@@ -590,9 +602,10 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
 
 int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int nmat) {
     CK(cudaSetDevice(dev));
-    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    drop_graphs();
     gm_k_est = 0;
     gm_k_seen = 0;
+    gm_rate[0] = gm_rate[1] = 0.0;
     if (nmat < 0 || nmat > QMS_MAX_SLOTS - 1) { err = "nmat must be in 0..255"; return QMS_ERR_ARG; }
     const long long ncell = (long long)g.xs * g.ys * g.zs;
     if (host_slots) {
@@ -617,12 +630,12 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
             int rc;
             if (fp64_inner) {
                 QmsMG<double>& M = mgd[tr];
-                M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = desc.mg_omega;
+                M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = desc.mg_omega; M.alpha = desc.mg_alpha;
                 rc = M.build(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, tr == 1), vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             } else {
                 QmsMG<float>& M = mgf[tr];
-                M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = (float)desc.mg_omega;
+                M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = (float)desc.mg_omega; M.alpha = (float)desc.mg_alpha;
                 rc = M.build(g, coef32(), qms_step_par<float>(g, 0, 0, 0, desc.dt, tr == 1), (float)vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             }
@@ -673,6 +686,9 @@ template void QmsSolver::op<float>(bool, int, const QStepPar<float>&, const floa
                                    const float*, double*);
 
 const CUtensorMap& QmsSolver::tmap(const void* p) const { return tmaps.at(p); }
+const CUtensorMap& QmsSolver::tmapq(const void* p, int qs) const {
+    return qs == 1 ? tmapsA.at(p) : (qs == 2 ? tmapsV.at(p) : tmaps.at(p));
+}
 
 template <typename T>
 void QmsSolver::op_pl(bool adv, int mode, const QStepPar<T>& P, const T* xin, T* y, const T* w, double* partials) {
@@ -749,16 +765,34 @@ int QmsSolver::read_scalars() {
 }
 
 template <typename T>
-void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool transient, bool jacobi_pcg) {
+void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool transient, bool jacobi_pcg,
+                        const QStepPar<T>* P, bool adv) {
     if (use_mg) {
         OpEv* ev = prof_begin(2, 0.0);
-        if (sizeof(T) == 4)
-            nlaunch += mgf[transient ? 1 : 0].vcycle((const float*)r, bscale != nullptr, (float*)z, tmap(z),
-                                                     (float*)mgtmp, tmap(mgtmp), cmap32, mask_v, status, st);
-        else
-            nlaunch += mgd[transient ? 1 : 0].vcycle((const double*)r, bscale != nullptr, (double*)z, tmap(z),
-                                                     (double*)mgtmp, tmap(mgtmp), cmap64, mask_v, status, st);
-        if (!mask_v) regions.apply<T>(r, bscale, z, st, nlaunch);
+        const bool f32 = sizeof(T) == 4;
+        const CUtensorMap& cm = f32 ? cmap32 : cmap64;
+        auto cycle = [&](const T* b, int qs, const CUtensorMap& cmq) {
+            if (f32)
+                nlaunch += mgf[transient ? 1 : 0].vcycle((const float*)b, bscale != nullptr, (float*)z, tmapq(z, qs),
+                                                         mgtmp, tmapq(mgtmp, qs), cmq, mask_v, status, st, qs);
+            else
+                nlaunch += mgd[transient ? 1 : 0].vcycle((const double*)b, bscale != nullptr, (double*)z,
+                                                         tmapq(z, qs), (double*)mgtmp, tmapq(mgtmp, qs), cmq, mask_v,
+                                                         status, st, qs);
+        };
+        if (P && !mask_v && bscale && desc.mg_coupling == 1) {
+            // lower block-triangular: the A blocks first, then the V block on the residual that
+            // the A correction leaves in the V rows (row-scaled like r)
+            T* tv = (T*)mgtmp2;
+            cycle(r, 1, cm);
+            qms_launch_op_pl<T>(g, *P, tmap(z), cm, adv, QOPH_VCOUPLE, tv, r, nullptr, status, st);
+            cycle(tv, 2, f32 ? cmapV32 : cmapV64);
+            nlaunch++;
+            regions.apply<T>(tv, bscale, z, st, nlaunch);
+        } else {
+            cycle(r, 0, cm);
+            if (!mask_v) regions.apply<T>(r, bscale, z, st, nlaunch);
+        }
         prof_end(ev);
     } else if (jacobi_pcg) {
         qk_jacobi<T><<<(int)vec_blocks, 256, 0, st>>>(npl, mask_v ? 3 * qms_pl(g).comp : npl, r,
@@ -787,12 +821,12 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
     for (int it = 0; it < desc.max_inner; it++) {
         qk_bicg_p<T><<<vb, 256, 0, st>>>(n, r, p, vv, S);
         nlaunch++;
-        if (use_mg) precond<T>(p, dg, y, false, transient, false);
+        if (use_mg) precond<T>(p, dg, y, false, transient, false, &P, adv);
         op_pl<T>(adv, QOPH_SCALED, P, y, vv, rh, part);
         finalize(FIN_BICG_ALPHA, 1, nbop);
         qk_bicg_s<T><<<vb, 256, 0, st>>>(n, r, vv, s, S);
         nlaunch++;
-        if (use_mg) precond<T>(s, dg, z, false, transient, false);
+        if (use_mg) precond<T>(s, dg, z, false, transient, false, &P, adv);
         op_pl<T>(adv, QOPH_SCALED, P, z, t, s, part);
         finalize(FIN_BICG_OMEGA, 2, nbop);
         qk_bicg_xr<T><<<vb, 256, 0, st>>>(n, y, z, s, t, rh, e, r, S, part);
@@ -839,7 +873,7 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
     for (int j = 0; j < kmax; j++) {
         T* vj = (T*)gmV[j];
         T* zj = use_mg ? (T*)gmZ[j] : vj;
-        if (use_mg) precond<T>(vj, dg, zj, false, transient, false);
+        if (use_mg) precond<T>(vj, dg, zj, false, transient, false, &P, adv);
         op_pl<T>(adv, QOPH_SCALED, P, zj, w, nullptr, nullptr);
         gm_dots<T>(j + 1, vb, st, n, Vp, w, part);
         qk_gm_hcol<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H);
@@ -919,18 +953,38 @@ int QmsSolver::residual(bool adv, bool transient, const double v[3]) {
 
 // One refinement iteration (FGMRES with k iterations, FP64 update, FP64 residual) as a
 // CUDA graph, captured once per (velocity, form, k) and replayed.
+void QmsSolver::drop_graphs() {
+    for (IrGraph& G : graphs) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        for (auto& e : G.ev) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    }
+    graphs.clear();
+}
+
 int QmsSolver::ir_iteration_graph(bool adv, bool transient, const double v[3], int k) {
     const bool want_prof = prof && !graph_prof_broken;
-    const bool same = graph_exec && graph_k == k && graph_tr == transient && graph_adv == adv &&
-                      graph_v[0] == v[0] && graph_v[1] == v[1] && graph_v[2] == v[2] && graph_prof == want_prof;
-    if (!same) {
-        if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    IrGraph* G = nullptr;
+    for (IrGraph& e : graphs)
+        if (e.k == k && e.tr == transient && e.adv == adv && e.v[0] == v[0] && e.v[1] == v[1] && e.v[2] == v[2] &&
+            e.prof == want_prof) { G = &e; break; }
+    if (!G) {
+        // a small cache: the least recently used capture makes room
+        constexpr size_t kMaxGraphs = 6;
+        if (graphs.size() >= kMaxGraphs) {
+            size_t lru = 0;
+            for (size_t q = 1; q < graphs.size(); q++) if (graphs[q].used < graphs[lru].used) lru = q;
+            if (graphs[lru].exec) cudaGraphExecDestroy(graphs[lru].exec);
+            for (auto& e : graphs[lru].ev) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+            graphs.erase(graphs.begin() + (long)lru);
+        }
+        graphs.emplace_back();
+        G = &graphs.back();
         // with profiling on, the operator / V-cycle event records are captured as graph nodes
-        // on their own event set and read back after every replay
+        // on the entry's own event set and read back after every replay
         const bool prof_was = prof;
         const size_t ev_saved = evused;
         prof = want_prof;
-        std::swap(evpool, graph_ev);
+        std::swap(evpool, G->ev);
         evused = 0;
         capturing = true;
         const long long n0 = nlaunch;
@@ -944,28 +998,34 @@ int QmsSolver::ir_iteration_graph(bool adv, bool transient, const double v[3], i
         cudaGraph_t graph = nullptr;
         if (e == cudaSuccess) e = cudaStreamEndCapture(st, &graph);
         capturing = false;
-        graph_evn = evused;
-        std::swap(evpool, graph_ev);
+        G->evn = evused;
+        std::swap(evpool, G->ev);
         evused = ev_saved;
         prof = prof_was;
-        if (rc) return rc;
-        if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return QMS_ERR_CUDA; }
-        e = cudaGraphInstantiate(&graph_exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) { err = std::string("graph instantiate: ") + cudaGetErrorString(e); return QMS_ERR_CUDA; }
-        graph_launches = nlaunch - n0;
+        if (rc == 0 && e == cudaSuccess) e = cudaGraphInstantiate(&G->exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (rc || e != cudaSuccess) {
+            if (G->exec) cudaGraphExecDestroy(G->exec);
+            for (auto& q : G->ev) { cudaEventDestroy(q.a); cudaEventDestroy(q.b); }
+            graphs.pop_back();
+            if (rc) return rc;
+            err = std::string("graph capture: ") + cudaGetErrorString(e);
+            return QMS_ERR_CUDA;
+        }
+        G->launches = nlaunch - n0;
         nlaunch = n0;
-        graph_k = k; graph_tr = transient; graph_adv = adv; graph_prof = want_prof;
-        graph_v[0] = v[0]; graph_v[1] = v[1]; graph_v[2] = v[2];
+        G->k = k; G->tr = transient; G->adv = adv; G->prof = want_prof;
+        G->v[0] = v[0]; G->v[1] = v[1]; G->v[2] = v[2];
     }
-    CK(cudaGraphLaunch(graph_exec, st));
-    nlaunch += graph_launches;
+    G->used = ++graph_clock;
+    CK(cudaGraphLaunch(G->exec, st));
+    nlaunch += G->launches;
     last_inner = 2;
     last_gm_k = k;
     int rc = read_scalars();                     // synchronises the stream
-    if (rc == 0 && graph_prof && prof)
-        for (size_t q = 0; q < graph_evn; q++)
-            if (!prof_accum(graph_ev[q])) { graph_prof_broken = true; break; }
+    if (rc == 0 && G->prof && prof)
+        for (size_t q = 0; q < G->evn; q++)
+            if (!prof_accum(G->ev[q])) { graph_prof_broken = true; break; }
     return rc;
 }
 
@@ -986,6 +1046,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     graph_resid_ready = false;
     const int gm_m = std::min(desc.gmres_m, GM_MAXM);
     int graph_k_used = 0;                 // k of the graph replay that produced this residual (0: none)
+    int gm_k_last = 0;                    // FGMRES steps of the last cycle (graph or host-checked)
     double best_rn = INFINITY, best_rel = INFINITY;
     for (;;) {
         int rc = 0;
@@ -1005,19 +1066,18 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         if (outer == 0) stats.initial_residual = rel;
         if (!std::isfinite(rel)) { stats.status |= QMS_ST_NAN; break; }
         if (rel <= desc.tol || rn == 0.0) break;
-        // A replayed iteration runs a fixed number k of FGMRES steps.  If it missed the inner
-        // target, raise k for the next replay to what the observed per-step rate needs
-        // (k log(target) / log(rho)); such a miss is not a stall while k can still grow.
+        // Per-step reduction rate of FGMRES, from the true residuals around each cycle; the
+        // slower of the last two cycles sizes the next replay.  A replay that gained less than a
+        // tenth per cycle while k can still grow is not a stall.
         bool k_limited = false;
-        if (graph_k_used > 0 && prev_rn > 0 && rn > 0 && rn < prev_rn) {
+        if (gm_k_last > 0 && std::isfinite(prev_rn) && prev_rn > 0 && rn > 0 && rn < prev_rn) {
             const double rho = rn / prev_rn;
-            if (rho > desc.inner_rtol && graph_k_used < gm_m) {
-                const double need = graph_k_used * std::log(desc.inner_rtol) / std::log(std::min(rho, 0.999));
-                gm_k_est = std::min(gm_m, std::max(graph_k_used + 1, (int)std::ceil(need)));
-                k_limited = true;
-            }
+            gm_rate[1] = gm_rate[0];
+            gm_rate[0] = std::pow(rho, 1.0 / gm_k_last);
+            if (graph_k_used > 0 && graph_k_used < gm_m && rho > 0.1) k_limited = true;
         }
         graph_k_used = 0;
+        gm_k_last = 0;
         // Stall: near the round-off floor (within 1e3 of the tolerance) two iterations without
         // halving the residual end the solve; elsewhere only three iterations that gain less
         // than 10 % do, so that slowly but steadily converging solves continue.
@@ -1057,11 +1117,21 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
             rc = fp64_inner ? inner_bicgstab<double>(adv, transient, v, it)
                             : inner_bicgstab<float>(adv, transient, v, it);
         } else if (desc.use_graphs && gm_k_est > 0) {
-            // replay the captured refinement iteration; its residual is read back with it
+            // replay a captured refinement iteration; its residual is read back with it.  k is
+            // the count that, at the observed rate, reaches 0.3 tol in as few cycles as m steps
+            // per cycle allow, spread evenly over those cycles
             it = gm_k_est;
-            rc = ir_iteration_graph(adv, transient, v, gm_k_est);
+            const double rate = std::max(gm_rate[0], gm_rate[1]);
+            const double goal = 0.3 * desc.tol / rel;
+            if (rate > 0.0 && rate < 0.995 && goal < 1.0) {
+                const double lr = std::log(rate);
+                const int cyc = std::max(1, (int)std::ceil(std::log(goal) / (gm_m * lr)));
+                it = std::min(gm_m, std::max(6, (int)std::ceil(std::log(goal) / (cyc * lr)) + 1));
+            }
+            rc = ir_iteration_graph(adv, transient, v, it);
             if (rc) return rc;
             graph_k_used = it;
+            gm_k_last = it;
             stats.inner_iterations += it;
             outer++;
             graph_resid_ready = true;
@@ -1070,6 +1140,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
             last_inner = 2;
             rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it, 0) : inner_gmres<float>(adv, transient, v, it, 0);
             if (!rc) gm_k_seen = std::max(gm_k_seen, it);
+            gm_k_last = it;
         }
         if (rc) return rc;
         stats.inner_iterations += it;
@@ -1117,5 +1188,7 @@ template int QmsSolver::inner_pcg<float>(bool, int&);
 template int QmsSolver::inner_pcg<double>(bool, int&);
 template int QmsSolver::inner_gmres<float>(bool, bool, const double*, int&, int);
 template int QmsSolver::inner_gmres<double>(bool, bool, const double*, int&, int);
-template void QmsSolver::precond<float>(const float*, const float*, float*, bool, bool, bool);
-template void QmsSolver::precond<double>(const double*, const float*, double*, bool, bool, bool);
+template void QmsSolver::precond<float>(const float*, const float*, float*, bool, bool, bool,
+                                        const QStepPar<float>*, bool);
+template void QmsSolver::precond<double>(const double*, const float*, double*, bool, bool, bool,
+                                         const QStepPar<double>*, bool);

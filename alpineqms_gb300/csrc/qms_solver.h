@@ -46,13 +46,16 @@ struct QmsSolver {
     float* dg_tr = nullptr;
     void* vec[QMS_NVEC] = {};   // inner Krylov vectors (FP32 or FP64)
     float* mgtmp = nullptr;     // level-0 Jacobi temporary of the multigrid
+    float* mgtmp2 = nullptr;    // V right-hand side of the block-triangular preconditioner
     QmsMG<float> mgf[2];        // hierarchies of the steady [0] and transient [1] operators (mixed)
     QmsMG<double> mgd[2];       // the same in FP64 (plain FP64 solver)
     bool use_mg = false;
     QmsRegions regions;         // conductor-region coarse space of the V block (with MG)
     // z = preconditioner(r): multigrid on (bscale .* r) or the Jacobi / identity fallback
+    // With P (transient rows of the unmasked system, desc.mg_coupling = 1) the multigrid is
+    // lower block-triangular in (A, V): z_A = MG_A(r_A), z_V = MG_V(r_V - D_V^-1 M_VA z_A).
     template <typename T> void precond(const T* r, const float* bscale, T* z, bool mask_v, bool transient,
-                                       bool jacobi_pcg);
+                                       bool jacobi_pcg, const QStepPar<T>* P = nullptr, bool adv = false);
 
     qms_stats stats{};
     std::string err;
@@ -67,9 +70,7 @@ struct QmsSolver {
     std::vector<OpEv> evpool;
     size_t evused = 0;
     bool capturing = false;                      // event records go into a graph being captured
-    std::vector<OpEv> graph_ev;                  // event records inside the captured graph
-    size_t graph_evn = 0;
-    bool graph_prof = false, graph_prof_broken = false;
+    bool graph_prof_broken = false;
     qms_profile profacc{};
     int profile_enable(bool on);
     int profile_collect(qms_profile* out);
@@ -81,7 +82,10 @@ struct QmsSolver {
     long long npl = 0;                              // padded inner-vector length
     std::unordered_map<const void*, CUtensorMap> tmaps;   // tensor maps of the padded vectors
     CUtensorMap cmap32{}, cmap64{};                 // ... and of the node coefficients
+    std::unordered_map<const void*, CUtensorMap> tmapsA, tmapsV;   // ... of their A blocks / V block
+    CUtensorMap cmapV32{}, cmapV64{};               // ... of the three conductivities
     const CUtensorMap& tmap(const void* p) const;
+    const CUtensorMap& tmapq(const void* p, int qs) const;
 
     ~QmsSolver();
     void release();
@@ -102,14 +106,25 @@ struct QmsSolver {
     template <typename T> int inner_gmres(bool adv, bool transient, const double v[3], int& iters, int fixed_k);
     void residual_launch(bool adv, bool transient, const double v[3]);
     int ir_iteration_graph(bool adv, bool transient, const double v[3], int k);
-    cudaGraphExec_t graph_exec = nullptr;
-    int graph_k = 0;
-    bool graph_tr = false, graph_adv = false;
-    double graph_v[3] = {0, 0, 0};
-    long long graph_launches = 0;
+    // captured refinement iterations, one per FGMRES count k (and step parameters); the
+    // profile event records of a capture belong to its entry
+    struct IrGraph {
+        cudaGraphExec_t exec = nullptr;
+        int k = 0;
+        bool tr = false, adv = false, prof = false;
+        double v[3] = {0, 0, 0};
+        long long launches = 0;
+        std::vector<OpEv> ev;
+        size_t evn = 0;
+        unsigned long long used = 0;
+    };
+    std::vector<IrGraph> graphs;
+    unsigned long long graph_clock = 0;
+    void drop_graphs();
     bool graph_resid_ready = false;
     int gm_k_est = 0;           // FGMRES iterations replayed per refinement iteration (0: not yet known)
     int gm_k_seen = 0;          // largest count seen while running with host checks
+    double gm_rate[2] = {0, 0}; // per-iteration residual reduction of the last two FGMRES cycles
     void* gmV[33] = {};         // FGMRES basis (m + 1) and preconditioned directions (m)
     void* gmZ[32] = {};
     double* gm_H = nullptr;     // Hessenberg matrix (m+1) x m, row-major with stride m

@@ -88,18 +88,20 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
 }
 
 // ---------------------------------------------------------------- tiles
-// A plane of the x tile: the four blocks, rows j0-1 .. j0+8, columns i0-1 .. i0+34 (36
-// columns: the box width must be a multiple of 16 bytes); coefficient plane: six arrays,
-// rows j0-1 .. j0+7.  Slots are padded to 128 bytes.
+// A plane of the x tile: NQ blocks (all four, or a subset), rows j0-1 .. j0+8, columns
+// i0-1 .. i0+34 (36 columns: the box width must be a multiple of 16 bytes); coefficient plane:
+// NC arrays (all six, or the three conductivities), rows j0-1 .. j0+7.  Slots are padded to
+// 128 bytes.
 #define PLX 36
 #define PLXY 10
 #define PLCY 9
-template <typename T>
+template <typename T, int NQ = 4, int NC = 6>
 struct PLTiles {
-    static constexpr int XSLOT = 4 * PLXY * PLX;                          // elements per x plane
-    static constexpr int CSLOT_RAW = 6 * PLCY * PLX;
+    static constexpr int XSLOT_RAW = NQ * PLXY * PLX;                     // elements per x plane
+    static constexpr int XSLOT = ((XSLOT_RAW * (int)sizeof(T) + 127) / 128) * 128 / (int)sizeof(T);
+    static constexpr int CSLOT_RAW = NC * PLCY * PLX;
     static constexpr int CSLOT = ((CSLOT_RAW * (int)sizeof(T) + 127) / 128) * 128 / (int)sizeof(T);
-    static constexpr unsigned XBYTES = XSLOT * sizeof(T);
+    static constexpr unsigned XBYTES = XSLOT_RAW * sizeof(T);
     static constexpr unsigned CBYTES = CSLOT_RAW * sizeof(T);
     static constexpr size_t SMEM = (size_t)(4 * XSLOT + 3 * CSLOT) * sizeof(T);
 };

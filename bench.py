@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 step comparison")
     ap.add_argument("--check-every", type=int, default=None)
+    ap.add_argument("--set", action="append", default=[], metavar="FIELD=VALUE",
+                    help="override a qms_desc field of the timed solver (e.g. gmres_m=24, mg_alpha=1.8)")
     return ap.parse_args()
 
 
@@ -259,6 +261,9 @@ def run_gpu(args):
     kw = {}
     if args.check_every:
         kw["check_every"] = args.check_every
+    for item in args.set:
+        key, _, val = item.partition("=")
+        kw[key] = float(val) if any(ch in val for ch in ".eE") else int(val)
     desc = default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt, precision=args.precision,
                         device=local, **kw)
     solver = QMSSolver(desc)

@@ -97,6 +97,11 @@ typedef struct {
                                 its region-stiffness-scaled Galerkin matrix at or below this are
                                 dropped (0 = automatic: 1e-9 with FP64 inner vectors, 1e-6 with FP32;
                                 negative = no region space) */
+    double mg_alpha;         /* scale of every coarse-grid correction of the V-cycle (over-correction
+                                of the piecewise-constant aggregation prolongation; <= 0 means 1) */
+    int mg_coupling;         /* transient steps: 1 (default) lower block-triangular preconditioner in
+                                (A, V) -- a cycle on the A blocks, then one on the V block for the
+                                residual the A correction leaves in the V rows; 0 block-diagonal */
 } qms_desc;
 
 typedef struct {
