@@ -42,8 +42,8 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->check_every = 2;
     d->device = 0;
     d->precond = QMS_PRECOND_MG;
-    d->mg_sweeps = 2;
-    d->mg_omega = 0.8;
+    d->mg_sweeps = 3;
+    d->mg_omega = 0.85;
     d->mg_vshift = 0.0;
     d->krylov = QMS_KRYLOV_GMRES;
     d->gmres_m = 32;
@@ -247,7 +247,7 @@ int qms_residual_norm(qms_handle* h, int transient, const double v[3], double* r
     QmsSolver& s = h->s;
     CKH(cudaSetDevice(s.dev));
     const bool adv = v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
-    int rc = s.residual(adv, transient != 0, v);
+    int rc = s.residual(adv, transient != 0, v, true);
     if (rc) return rc;
     double xn = std::sqrt(s.hS[0 + 2] + s.hS[0 + 3]);
     double rn = std::sqrt(s.hS[0] + s.hS[1]);

@@ -9,6 +9,7 @@
 // four rows from shared memory (qms_op_rows.cuh).  The only per-thread global traffic is
 // the output row (and the optional dot vector).
 #include "qms_internal.h"
+#include "qms_df.cuh"
 #include "qms_op_rows.cuh"
 #include "qms_pl.h"
 #include "qms_tile.cuh"
@@ -61,13 +62,15 @@ __device__ __forceinline__ T pl_div(T a, T d) {
     else return a / d;
 }
 
-// MODE: QOPH_APPLY (y = M x), QOPH_SCALED (y = D^-1 M x) or QOPH_VCOUPLE (V rows only:
-// y = w - D^-1 M (x_A, 0)); partials (optional, FP64, not with VCOUPLE): [0] += y . w (w may
-// be null), [1] += y . y
-template <typename T, bool ADV, int MODE>
+// MODE: QOPH_APPLY (y = M x), QOPH_SCALED (y = D^-1 M x), QOPH_VCOUPLE (V rows only:
+// y = w - D^-1 M (x_A, 0)) or QOPH_RESID (T = qdf: y = (float) (w - D^-1 M x), the refinement
+// residual in double-float arithmetic, with w the residual of the anchor and x the change of
+// the solution since then).  Partials (optional, FP64 across warps): APPLY / SCALED [0] += y . w
+// (w may be null), [1] += y . y; RESID |r_A|^2, |r_V|^2; none with VCOUPLE.
+template <typename T, bool ADV, int MODE, typename YT = T, typename WT = T>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap,
-         T* __restrict__ y, const T* __restrict__ w, double* __restrict__ partials, unsigned* __restrict__ err) {
+         YT* __restrict__ y, const WT* __restrict__ w, double* __restrict__ partials, unsigned* __restrict__ err) {
     using TL = PLTiles<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][4][PLXY][PLX]
@@ -118,15 +121,23 @@ qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const
     using RT = float;
     RT red0 = 0, red1 = 0;
     auto emit = [&](long long row, T acc, T diag, bool is_a, T) {
-        if (MODE == QOPH_VCOUPLE) {           // the A rows are not wanted (dead code)
+        if constexpr (MODE == QOPH_RESID) {
+            const T out = w[row] - acc / diag;
+            y[row] = out.h;
+            if (partials) {
+                const float o = out.h;
+                if (is_a) red0 += o * o;
+                else red1 += o * o;
+            }
+        } else if constexpr (MODE == QOPH_VCOUPLE) {   // the A rows are not wanted (dead code)
             if (!is_a) y[row] = w[row] - pl_div(acc, diag);
-            return;
-        }
-        const T out = MODE == QOPH_APPLY ? acc : pl_div(acc, diag);
-        y[row] = out;
-        if (partials) {
-            if (w) red0 += (RT)(out * w[row]);
-            red1 += (RT)(out * out);
+        } else {
+            const T out = MODE == QOPH_APPLY ? acc : pl_div(acc, diag);
+            y[row] = out;
+            if (partials) {
+                if (w) red0 += (RT)(out * w[row]);
+                red1 += (RT)(out * out);
+            }
         }
     };
     for (int k = k0; k <= kend; k++) {
@@ -168,6 +179,67 @@ qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const
         double s1 = qBlockSum(red1, sh);
         if (qLinTid() == 0) partials[nb + bid] = s1;
     }
+}
+
+// dx = x - x0 (FP64 subtraction, reference order) as double-float in the padded layout, with
+// the partials |x_A|^2, |x_V|^2 at [2 nb + block] and [3 nb + block] (gridDim.x == nb)
+__global__ void __launch_bounds__(256) qk_delta_split(QGrid g, const double* __restrict__ x,
+                                                      const double* __restrict__ x0, qdf* __restrict__ dx,
+                                                      double* __restrict__ partials) {
+    const QPL L = qms_pl(g);
+    float xa = 0.f, xv = 0.f;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.Nn; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.Nx) + 1, j = (int)((t / g.Nx) % g.Ny) + 1, k = (int)(t / ((long long)g.Nx * g.Ny)) + 1;
+        const long long nd = qms_pl_node(g, L, i, j, k);
+        auto one = [&](long long ref, long long pl, float& acc) {
+            const double v = x[ref];
+            dx[pl] = qdf_split(v - x0[ref]);
+            const float f = qdf_split(v).h;
+            acc += f * f;
+        };
+        if (i <= g.xs) one(qAX(g, i, j, k), nd, xa);
+        if (j <= g.ys) one(qAY(g, i, j, k), L.comp + nd, xa);
+        if (k <= g.zs) one(qAZ(g, i, j, k), 2 * L.comp + nd, xa);
+        one(qV(g, i, j, k), 3 * L.comp + nd, xv);
+    }
+    __shared__ double sh[32];
+    const double sa = qBlockSum(xa, sh);
+    if (threadIdx.x == 0) partials[2 * (long long)gridDim.x + blockIdx.x] = sa;
+    const double sv = qBlockSum(xv, sh);
+    if (threadIdx.x == 0) partials[3 * (long long)gridDim.x + blockIdx.x] = sv;
+}
+
+// double -> double-float, reference unknown order -> padded layout; its high words also to hi
+// when given
+__global__ void qk_split_ref_pl(QGrid g, const double* __restrict__ src, qdf* __restrict__ dst,
+                                float* __restrict__ hi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > g.Nx) return;
+    const QPL L = qms_pl(g);
+    const long long t = qms_pl_node(g, L, i, j, k);
+    auto one = [&](long long ref, long long pl) {
+        const qdf v = qdf_split(src[ref]);
+        dst[pl] = v;
+        if (hi) hi[pl] = v.h;
+    };
+    if (i <= g.xs) one(qAX(g, i, j, k), t);
+    if (j <= g.ys) one(qAY(g, i, j, k), L.comp + t);
+    if (k <= g.zs) one(qAZ(g, i, j, k), 2 * L.comp + t);
+    one(qV(g, i, j, k), 3 * L.comp + t);
+}
+
+// elementwise double -> double-float (the node coefficients)
+__global__ void qk_split_flat(long long n, const double* __restrict__ src, qdf* __restrict__ dst) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dst[t] = qdf_split(src[t]);
+}
+
+// out = r * scale[0] (padded layout, FP32)
+__global__ void qk_pl_scale(long long n, const float* __restrict__ r, const double* __restrict__ scale,
+                            float* __restrict__ out) {
+    const float s = (float)scale[0];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        out[t] = r[t] * s;
 }
 
 // FP32 diagonal of the operator in the padded layout (Dirichlet rows 1)
@@ -255,6 +327,13 @@ static void op_pl_prepare() {
     cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
     cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
     cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    if constexpr (sizeof(T) == 4) {
+        const int shd = (int)PLTiles<qdf>::SMEM;
+        cudaFuncSetAttribute(qk_op_pl<qdf, false, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             shd);
+        cudaFuncSetAttribute(qk_op_pl<qdf, true, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             shd);
+    }
     done.fetch_or(bit, std::memory_order_acq_rel);
 }
 
@@ -284,6 +363,32 @@ template void qms_launch_op_pl<float>(const QGrid&, const QStepPar<float>&, cons
                                       bool, int, float*, const float*, double*, unsigned*, cudaStream_t);
 template void qms_launch_op_pl<double>(const QGrid&, const QStepPar<double>&, const CUtensorMap&, const CUtensorMap&,
                                        bool, int, double*, const double*, double*, unsigned*, cudaStream_t);
+
+void qms_launch_resid_df(const QGrid& g, const QStepPar<qdf>& P, const CUtensorMap& xmap, const CUtensorMap& cmap,
+                         bool adv, float* r, const qdf* b, double* partials, unsigned* err, cudaStream_t st) {
+    op_pl_prepare<float>();
+    const dim3 bs(OTX, OTY, 1), gs((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
+    const size_t shm = PLTiles<qdf>::SMEM;
+    if (adv) qk_op_pl<qdf, true, QOPH_RESID, float, qdf><<<gs, bs, shm, st>>>(g, P, xmap, cmap, r, b, partials, err);
+    else qk_op_pl<qdf, false, QOPH_RESID, float, qdf><<<gs, bs, shm, st>>>(g, P, xmap, cmap, r, b, partials, err);
+}
+
+void qms_launch_delta_split(const QGrid& g, const double* x, const double* x0, qdf* dx, double* partials,
+                            long long nb, cudaStream_t st) {
+    qk_delta_split<<<(unsigned)nb, 256, 0, st>>>(g, x, x0, dx, partials);
+}
+
+void qms_launch_split_ref_pl(const QGrid& g, const double* src, qdf* dst, float* hi, cudaStream_t st) {
+    qk_split_ref_pl<<<qms_node_grid(g), 128, 0, st>>>(g, src, dst, hi);
+}
+
+void qms_launch_split_flat(long long n, const double* src, qdf* dst, cudaStream_t st) {
+    qk_split_flat<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 16), 256, 0, st>>>(n, src, dst);
+}
+
+void qms_launch_pl_scale(long long n, const float* r, const double* scale, float* out, cudaStream_t st) {
+    qk_pl_scale<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 16), 256, 0, st>>>(n, r, scale, out);
+}
 
 void qms_launch_diag_pl(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st) {
     cudaMemsetAsync(dg, 0, qms_pl(g).n * sizeof(float), st);

@@ -2,6 +2,7 @@
 #pragma once
 #include "qms_internal.h"
 #include "qms_tma.cuh"
+#include "qms_df.cuh"
 
 dim3 qms_node_grid(const QGrid& g);                 // one thread per node: (ceil(Nx/128), Ny, Nz) x 128
 long long qms_op_pl_num_blocks(const QGrid& g);
@@ -11,6 +12,19 @@ long long qms_op_pl_num_blocks(const QGrid& g);
 template <typename T>
 void qms_launch_op_pl(const QGrid& g, const QStepPar<T>& P, const CUtensorMap& xmap, const CUtensorMap& cmap, bool adv,
                       int mode, T* y, const T* w, double* partials, unsigned* err, cudaStream_t st);
+
+// refinement residual in double-float from an anchor: r = (float) (r0 - D^-1 M dx) on padded
+// vectors, with r0 the anchor's scaled residual and dx (xmap) the change of x since the anchor,
+// both double-float, and the node coefficients (cmap) as double-float; partials |r_A|^2, |r_V|^2
+void qms_launch_resid_df(const QGrid& g, const QStepPar<qdf>& P, const CUtensorMap& xmap, const CUtensorMap& cmap,
+                         bool adv, float* r, const qdf* r0, double* partials, unsigned* err, cudaStream_t st);
+// dx = x - x0 as double-float (padded layout) and the partials |x_A|^2, |x_V|^2 of nb blocks
+void qms_launch_delta_split(const QGrid& g, const double* x, const double* x0, qdf* dx, double* partials,
+                            long long nb, cudaStream_t st);
+// ref -> padded double-float (and its high words to hi when given)
+void qms_launch_split_ref_pl(const QGrid& g, const double* src, qdf* dst, float* hi, cudaStream_t st);
+void qms_launch_split_flat(long long n, const double* src, qdf* dst, cudaStream_t st);
+void qms_launch_pl_scale(long long n, const float* r, const double* scale, float* out, cudaStream_t st);
 
 void qms_launch_diag_pl(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st);
 

@@ -474,8 +474,8 @@ void QmsSolver::release() {
     if (gm_H) cudaFree(gm_H);
     if (gm_scal) cudaFree(gm_scal);
     gm_H = gm_scal = nullptr;
-    void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,
-                    S,     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64};
+    void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
+                    status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -485,6 +485,7 @@ void QmsSolver::release() {
     if (st && own_stream) cudaStreamDestroy(st);
     ids = nullptr; dtab64 = nullptr; dtab32 = nullptr; x = b = r64 = H = slicebuf = part = S = nullptr;
     status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; mgtmp2 = nullptr; xbest = nullptr;
+    xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -561,6 +562,19 @@ int QmsSolver::init(const qms_desc& d) {
     for (int i = 0; i <= GM_MAXM; i++) if (gmV[i]) mapped.push_back(gmV[i]);
     for (int i = 0; i < GM_MAXM; i++) if (gmZ[i]) mapped.push_back(gmZ[i]);
     if (mgtmp2) mapped.push_back(mgtmp2);
+    if (!fp64_inner) {
+        df_resid = true;
+        CK(pl_alloc((void**)&xdf, 8));
+        CK(pl_alloc((void**)&r0df, 8));
+        CK(cudaMalloc(&x0, n * 8));
+        CK(pl_alloc((void**)&rpl, 4));
+        CK(cudaMalloc(&ncdf, 6 * qms_pl(g).comp * 8));
+        CK(cudaMemsetAsync(ncdf, 0, 6 * qms_pl(g).comp * 8, st));
+        if (!qms_make_pl_map(&xdfmap, xdf, g, 8, 4, PLXY) || !qms_make_pl_map(&cdfmap, ncdf, g, 8, 6, PLCY)) {
+            err = "tensor map encoding failed";
+            return QMS_ERR_CUDA;
+        }
+    }
     const long long vbytes = 3 * qms_pl(g).comp * (long long)tsize;   // offset of the V block
     for (const void* p : mapped) {
         CUtensorMap mp, ma, mv;
@@ -586,8 +600,10 @@ int QmsSolver::init(const qms_desc& d) {
 size_t qms_device_bytes_impl(const qms_desc& d) {
     QGrid g = qms_make_grid(d.xs, d.ys, d.zs, d.dx, d.dy, d.dz);
     size_t ts = d.precision == QMS_PREC_FP64 ? 8 : 4;
-    // the block-triangular preconditioner's V right-hand side
+    // the block-triangular preconditioner's V right-hand side; the double-float residual's x, b,
+    // coefficients and FP32 result (mixed precision)
     size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
+    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4) + 6 * qms_pl(g).comp * 8 + g.n * 8;
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
@@ -605,7 +621,8 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     drop_graphs();
     gm_k_est = 0;
     gm_k_seen = 0;
-    gm_rate[0] = gm_rate[1] = 0.0;
+    gm_lrate[0] = gm_lrate[1] = 0.0;
+    gm_k_fine = false;
     if (nmat < 0 || nmat > QMS_MAX_SLOTS - 1) { err = "nmat must be in 0..255"; return QMS_ERR_ARG; }
     const long long ncell = (long long)g.xs * g.ys * g.zs;
     if (host_slots) {
@@ -620,6 +637,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     // node coefficients, then the Jacobi diagonals (velocity does not enter the diagonal)
     qms_launch_node_coef<float>(g, coef32(), nc32, st);
     qms_launch_node_coef<double>(g, coef64(), nc64, st);
+    if (df_resid) qms_launch_split_flat(6 * qms_pl(g).comp, nc64, ncdf, st);
     QCoef<float> c32 = coef32();
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
@@ -812,9 +830,9 @@ int QmsSolver::inner_bicgstab(bool adv, bool transient, const double v[3], int& 
     const float* dg = transient ? dg_tr : dg_steady;
     QStepPar<T> P = qms_step_par<T>(g, v[0], v[1], v[2], desc.dt, transient);
     const int vb = (int)vec_blocks;
-    qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, r, st);
+    resid_to_inner<T>(r);
     qk_bicg_init<T><<<vb, 256, 0, st>>>(n, r, rh, p, vv, e, part);
-    nlaunch += 2;
+    nlaunch++;
     finalize(FIN_BICG_INIT, 1, vec_blocks);
     const double tol2 = desc.inner_rtol * desc.inner_rtol;
     iters = 0;
@@ -866,8 +884,8 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
     for (int i = 0; i < m; i++) Zp.p[i] = use_mg ? gmZ[i] : gmV[i];
     T* w = (T*)vec[0];
     qk_gm_reset<<<1, 128, 0, st>>>(m, gm_scal);
-    qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, (T*)gmV[0], st);
-    nlaunch += 2;
+    resid_to_inner<T>((T*)gmV[0]);
+    nlaunch++;
     const double tol = desc.inner_rtol;
     int k = 0;
     for (int j = 0; j < kmax; j++) {
@@ -906,9 +924,9 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
     QStepPar<T> P = qms_step_par<T>(g, 0, 0, 0, desc.dt, transient);
     const int vb = (int)vec_blocks;
     // V block frozen at zero: the steady magnetostatic system with v = 0 has V = 0
-    qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, r, st);
+    resid_to_inner<T>(r);
     qk_cg_init<T><<<vb, 256, 0, st>>>(n, dg, r, e);
-    nlaunch += 2;
+    nlaunch++;
     precond<T>(r, nullptr, z, true, transient, true);
     qk_cg_dot<T><<<vb, 256, 0, st>>>(n, r, z, p, part);
     nlaunch++;
@@ -939,14 +957,45 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
     return 0;
 }
 
-void QmsSolver::residual_launch(bool adv, bool transient, const double v[3]) {
-    QStepPar<double> P = qms_step_par<double>(g, v[0], v[1], v[2], desc.dt, transient);
-    op<double>(adv, QOPH_RESID, P, x, b, r64, nullptr, part);
+void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], bool exact) {
+    if (df_resid && anchor_ready && !exact) {
+        // double-float from the anchor: dx = x - x0 split into the padded layout (with the |x|^2
+        // partials), then the TMA-staged stencil on the FP32 pipe
+        OpEv* ev = prof_begin(3, (double)g.n * 8 * 4 + (double)g.xs * g.ys * g.zs);
+        qms_launch_delta_split(g, x, x0, xdf, part, nbop, st);
+        qms_launch_resid_df(g, qms_step_par<qdf>(g, v[0], v[1], v[2], desc.dt, transient), xdfmap, cdfmap, adv, rpl,
+                            r0df, part, status, st);
+        nlaunch += 2;
+        prof_end(ev);
+    } else {
+        QStepPar<double> P = qms_step_par<double>(g, v[0], v[1], v[2], desc.dt, transient);
+        op<double>(adv, QOPH_RESID, P, x, b, r64, nullptr, part);
+        if (df_resid) {
+            // the anchor of the double-float residuals that follow in this solve
+            qms_launch_split_ref_pl(g, r64, r0df, rpl, st);
+            cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st);
+            nlaunch++;
+            anchor_ready = true;
+        }
+    }
     finalize(FIN_RESID, 4, nbop);
 }
 
-int QmsSolver::residual(bool adv, bool transient, const double v[3]) {
-    residual_launch(adv, transient, v);
+template <typename T>
+void QmsSolver::resid_to_inner(T* out) {
+    if constexpr (sizeof(T) == 4) {
+        if (df_resid) {
+            qms_launch_pl_scale(npl, rpl, S + S_INVNRM, out, st);
+            nlaunch++;
+            return;
+        }
+    }
+    qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, out, st);
+    nlaunch++;
+}
+
+int QmsSolver::residual(bool adv, bool transient, const double v[3], bool exact) {
+    residual_launch(adv, transient, v, exact);
     CK(cudaGetLastError());
     return read_scalars();
 }
@@ -1036,6 +1085,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     for (int q = 0; q < 9; q++) ex.G[q] = G[q];
     // b from the previous solution (x); Dirichlet values written into x (warm start keeps them exact)
     qms_launch_rhs(g, ids, dtab64, ex, desc.dt, transient ? 1 : 0, x, b, x, st);
+    anchor_ready = false;          // the first residual of this solve is the FP64 anchor
     nlaunch++;
     CK(cudaMemsetAsync(status, 0, 4, st));
     const bool adv = v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
@@ -1047,6 +1097,8 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     const int gm_m = std::min(desc.gmres_m, GM_MAXM);
     int graph_k_used = 0;                 // k of the graph replay that produced this residual (0: none)
     int gm_k_last = 0;                    // FGMRES steps of the last cycle (graph or host-checked)
+    int gm_cycles = 0;                    // FGMRES cycles run in this solve
+    int graph_cycles = 0;                 // ... of them replayed from graphs
     double best_rn = INFINITY, best_rel = INFINITY;
     for (;;) {
         int rc = 0;
@@ -1066,14 +1118,16 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         if (outer == 0) stats.initial_residual = rel;
         if (!std::isfinite(rel)) { stats.status |= QMS_ST_NAN; break; }
         if (rel <= desc.tol || rn == 0.0) break;
-        // Per-step reduction rate of FGMRES, from the true residuals around each cycle; the
-        // slower of the last two cycles sizes the next replay.  A replay that gained less than a
-        // tenth per cycle while k can still grow is not a stall.
+        // Per-step reduction rate of FGMRES from the true residuals around each cycle, kept
+        // apart for the first cycle of a solve and the later ones and smoothed in log space;
+        // it sizes the next replay.  A replay that gained less than a tenth per cycle while k
+        // can still grow is not a stall.
         bool k_limited = false;
         if (gm_k_last > 0 && std::isfinite(prev_rn) && prev_rn > 0 && rn > 0 && rn < prev_rn) {
             const double rho = rn / prev_rn;
-            gm_rate[1] = gm_rate[0];
-            gm_rate[0] = std::pow(rho, 1.0 / gm_k_last);
+            const double lr = std::log(rho) / gm_k_last;
+            double& slot = gm_lrate[gm_cycles == 1 ? 0 : 1];
+            slot = slot < 0.0 ? 0.5 * (slot + lr) : lr;
             if (graph_k_used > 0 && graph_k_used < gm_m && rho > 0.1) k_limited = true;
         }
         graph_k_used = 0;
@@ -1117,21 +1171,20 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
             rc = fp64_inner ? inner_bicgstab<double>(adv, transient, v, it)
                             : inner_bicgstab<float>(adv, transient, v, it);
         } else if (desc.use_graphs && gm_k_est > 0) {
-            // replay a captured refinement iteration; its residual is read back with it.  k is
-            // the count that, at the observed rate, reaches 0.3 tol in as few cycles as m steps
-            // per cycle allow, spread evenly over those cycles
+            // replay a captured refinement iteration; its residual is read back with it.  The
+            // first two cycles of a solve run gm_k_est steps each (tuned across solves so that two
+            // cycles just suffice); a further cycle runs what the observed rate of the later cycles
+            // needs to reach tol / 2
             it = gm_k_est;
-            const double rate = std::max(gm_rate[0], gm_rate[1]);
-            const double goal = 0.3 * desc.tol / rel;
-            if (rate > 0.0 && rate < 0.995 && goal < 1.0) {
-                const double lr = std::log(rate);
-                const int cyc = std::max(1, (int)std::ceil(std::log(goal) / (gm_m * lr)));
-                it = std::min(gm_m, std::max(6, (int)std::ceil(std::log(goal) / (cyc * lr)) + 1));
-            }
+            const double lgoal = std::log(0.5 * desc.tol / rel);
+            if (graph_cycles >= 2 && gm_lrate[1] < -1e-3 && lgoal < 0.0)
+                it = std::min(gm_m, std::max(6, (int)std::ceil(lgoal / gm_lrate[1]) + 2));
+            graph_cycles++;
             rc = ir_iteration_graph(adv, transient, v, it);
             if (rc) return rc;
             graph_k_used = it;
             gm_k_last = it;
+            gm_cycles++;
             stats.inner_iterations += it;
             outer++;
             graph_resid_ready = true;
@@ -1141,6 +1194,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
             rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it, 0) : inner_gmres<float>(adv, transient, v, it, 0);
             if (!rc) gm_k_seen = std::max(gm_k_seen, it);
             gm_k_last = it;
+            gm_cycles++;
         }
         if (rc) return rc;
         stats.inner_iterations += it;
@@ -1153,6 +1207,19 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     }
     if (!use_cg && desc.krylov == QMS_KRYLOV_GMRES && desc.use_graphs && gm_k_est == 0 && gm_k_seen > 0)
         gm_k_est = std::min(std::min(desc.gmres_m, GM_MAXM), gm_k_seen + 1);
+    // per-cycle count of the replays.  The FP32 inner solve gains little past ~1e-3 per cycle
+    // (its own rounding), so a longer cycle buys less than a restart from a fresh residual:
+    // probe downwards after every solve that two replays brought below tol / 3 (in steps of a
+    // fifth of k until the first solve that needed a third replay, one step after that), and
+    // step back up by two when a solve needed a third
+    if (graph_cycles > 0 && rel <= desc.tol) {
+        if (graph_cycles >= 3) {
+            gm_k_est = std::min(gm_m, gm_k_est + 2);
+            gm_k_fine = true;
+        } else if (graph_cycles == 2 && gm_cycles == 2 && rel < desc.tol / 3.0) {
+            gm_k_est = std::max(6, gm_k_est - (gm_k_fine ? 1 : std::max(1, gm_k_est / 5)));
+        }
+    }
     unsigned stt = 0;
     CK(cudaMemcpyAsync(&stt, status, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

@@ -4,6 +4,7 @@
 #include "qms_internal.h"
 #include "qms_mg.h"
 #include "qms_tma.cuh"
+#include "qms_df.cuh"
 
 #include <algorithm>
 #include <string>
@@ -47,6 +48,19 @@ struct QmsSolver {
     void* vec[QMS_NVEC] = {};   // inner Krylov vectors (FP32 or FP64)
     float* mgtmp = nullptr;     // level-0 Jacobi temporary of the multigrid
     float* mgtmp2 = nullptr;    // V right-hand side of the block-triangular preconditioner
+    // Mixed precision: the first residual of a solve (the anchor) is exact FP64; the later ones
+    // are r = r0 - D^-1 M (x - x0) in double-float on the FP32 pipe, from the anchor's residual r0
+    // and the change of x since the anchor state x0 (node coefficients split into float pairs,
+    // padded layout).  Every residual also lands in rpl (FP32, padded) for the inner solver.
+    bool df_resid = false;
+    bool anchor_ready = false;
+    double* x0 = nullptr;
+    qdf* xdf = nullptr;         // x - x0
+    qdf* r0df = nullptr;
+    qdf* ncdf = nullptr;
+    float* rpl = nullptr;
+    CUtensorMap xdfmap{}, cdfmap{};
+    template <typename T> void resid_to_inner(T* out);   // out = r / |r| in the inner precision
     QmsMG<float> mgf[2];        // hierarchies of the steady [0] and transient [1] operators (mixed)
     QmsMG<double> mgd[2];       // the same in FP64 (plain FP64 solver)
     bool use_mg = false;
@@ -92,7 +106,8 @@ struct QmsSolver {
     int init(const qms_desc& d);
     int set_materials(const uint8_t* host_slots, const double* rows6, int nmat);
     int solve(bool transient, const double v[3], const double B[3], const double G[9]);
-    int residual(bool adv, bool transient, const double v[3]);
+    // exact: the FP64 residual even where the double-float one would do (the public entry point)
+    int residual(bool adv, bool transient, const double v[3], bool exact = false);
     int fields(int which, int axis, int index, double* host_out);
     int finalize(int op, int nsum, long long nb);
     int read_scalars();
@@ -104,7 +119,7 @@ struct QmsSolver {
     template <typename T> int inner_bicgstab(bool adv, bool transient, const double v[3], int& iters);
     template <typename T> int inner_pcg(bool transient, int& iters);
     template <typename T> int inner_gmres(bool adv, bool transient, const double v[3], int& iters, int fixed_k);
-    void residual_launch(bool adv, bool transient, const double v[3]);
+    void residual_launch(bool adv, bool transient, const double v[3], bool exact = false);
     int ir_iteration_graph(bool adv, bool transient, const double v[3], int k);
     // captured refinement iterations, one per FGMRES count k (and step parameters); the
     // profile event records of a capture belong to its entry
@@ -124,7 +139,10 @@ struct QmsSolver {
     bool graph_resid_ready = false;
     int gm_k_est = 0;           // FGMRES iterations replayed per refinement iteration (0: not yet known)
     int gm_k_seen = 0;          // largest count seen while running with host checks
-    double gm_rate[2] = {0, 0}; // per-iteration residual reduction of the last two FGMRES cycles
+    bool gm_k_fine = false;     // gm_k_est has overshot downwards once: tune it in single steps
+    // log of the per-iteration residual reduction of FGMRES, smoothed over solves: [0] the first
+    // cycle of a solve, [1] the later ones (which start from a residual rich in slow modes)
+    double gm_lrate[2] = {0, 0};
     void* gmV[33] = {};         // FGMRES basis (m + 1) and preconditioned directions (m)
     void* gmZ[32] = {};
     double* gm_H = nullptr;     // Hessenberg matrix (m+1) x m, row-major with stride m
