@@ -847,6 +847,8 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     }
     MG0(2, x, nullptr, lv[1].b);
     launches++;
+    // levels >= 1: nu_coarse sweeps on each side when set
+    const int nuc1 = nu_coarse > 0 ? nu_coarse : nu1, nuc2 = nu_coarse > 0 ? nu_coarse : nu2;
     for (int l = 1; l < nl; l++) {
         MGLevelDev<T>& L = lv[l];
         if (l == nl - 1) {
@@ -858,7 +860,7 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
         T* tl = L.t;
         mg_smooth0<<<nblk(L.total), 256, 0, st>>>(L, L.b, nullptr, omega, xl, mv);
         launches++;
-        for (int s = 1; s < nu1; s++) {
+        for (int s = 1; s < nuc1; s++) {
             mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, L.b, nullptr, omega, xl, tl, mv);
             std::swap(xl, tl);
             launches++;
@@ -874,7 +876,7 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
         T* tl = L.t;
         mg_prolong<<<nblk(L.total), 256, 0, st>>>(L, xl, xl, lv[l + 1], lv[l + 1].x, alpha);
         launches++;
-        for (int s = 0; s < nu2; s++) {
+        for (int s = 0; s < nuc2; s++) {
             mg_smooth<<<nblk(L.total), 256, 0, st>>>(L, L.b, nullptr, omega, xl, tl, mv);
             std::swap(xl, tl);
             launches++;

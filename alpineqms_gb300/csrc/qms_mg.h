@@ -37,6 +37,7 @@ struct QmsMG {
     double* dminv = nullptr;       // dense FP64 inverses of the coarsest blocks
     long long* dmoff = nullptr;
     int nu1 = 2, nu2 = 2;
+    int nu_coarse = 0;             // sweeps on each side on levels >= 1 (0: nu1 / nu2)
     T omega = T(0.8);
     T alpha = T(1);
     int min_coarse = 5;

@@ -102,6 +102,8 @@ typedef struct {
     int mg_coupling;         /* transient steps: 1 (default) lower block-triangular preconditioner in
                                 (A, V) -- a cycle on the A blocks, then one on the V block for the
                                 residual the A correction leaves in the V rows; 0 block-diagonal */
+    int mg_coarse_sweeps;    /* Jacobi sweeps before and after the coarse correction on levels >= 1
+                                (0: mg_sweeps) */
 } qms_desc;
 
 typedef struct {
