@@ -1207,8 +1207,10 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         rel = best_rel;
         if (rel <= desc.tol) stats.status &= ~(unsigned)QMS_ST_NO_CONVERGENCE;
     }
+    // replays start short: a solve that needs a third cycle costs less than two long cycles,
+    // and the count below adapts either way
     if (!use_cg && desc.krylov == QMS_KRYLOV_GMRES && desc.use_graphs && gm_k_est == 0 && gm_k_seen > 0)
-        gm_k_est = std::min(std::min(desc.gmres_m, GM_MAXM), gm_k_seen + 1);
+        gm_k_est = std::min(std::min(desc.gmres_m, GM_MAXM), std::min(gm_k_seen + 1, 12));
     // per-cycle count of the replays.  The FP32 inner solve gains little past ~1e-3 per cycle
     // (its own rounding), so a longer cycle buys less than a restart from a fresh residual:
     // probe downwards after every solve that two replays brought below tol / 3 (in steps of a

@@ -311,3 +311,44 @@ def test_random_inclusions_32_vs_oracle(precision):
     j = o.edge_current_from_v(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, c, x)
     assert rel_l2(j, z["j_last"]) <= 1e-8, rel_l2(j, z["j_last"])
     s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", [dict(mg_coupling=0), dict(mg_coupling=1, mg_alpha=1.0),
+                                     dict(mg_coupling=1, mg_coarse_sweeps=2, mg_sweeps=2, mg_omega=0.8)],
+                         ids=["block-diagonal", "triangular-alpha1", "triangular-2sweeps"])
+def test_preconditioner_variants_match_direct_oracle(variant):
+    """The block-diagonal and lower block-triangular multigrid, with and without the
+    over-corrected coarse grid, all converge to the direct solution of the moving conductor."""
+    p, geom = _conductor_case(True)
+    ref = o.simulate(p, geom, steps=3, keep_states=True)
+    got = _run_gpu(p, geom, "mixed", 3, **variant)
+    oV = o.block_offsets(p["xs"], p["ys"], p["zs"])[3]
+    for (counter, xr, Hr), (x, H, st) in zip(ref, got):
+        assert st["status"] == 0
+        assert rel_l2(x[:oV], xr[:oV]) <= 1e-8, (counter, variant)
+        for q in range(3):
+            assert rel_l2(H[q], Hr[q]) <= 1e-8, (counter, q, variant)
+
+
+@pytest.mark.gpu
+def test_double_float_residual_agrees_with_fp64():
+    """The refinement's residual after the first iteration of a solve is evaluated in
+    double-float from an FP64 anchor; at the converged state it must agree with the exact FP64
+    residual of the same state (qms_residual_norm) to a few 1e-15 of |x|."""
+    p, geom = _conductor_case(True)
+    from alpineqms_gb300.trajectory import VelocitySchedule, scaled_field
+    from alpineqms_gb300.inputs import Trajectory
+    sched = VelocitySchedule([Trajectory(1, *t) for t in p["traj"]], p["dt"])
+    s = solver_for(p["xs"], p["ys"], p["zs"], (p["dx"], p["dy"], p["dz"]), p["dt"], geom, p["props"],
+                   precision="mixed")
+    B, G = scaled_field(p["B"], p["G"], p.get("excitation"), 0.0)
+    s.steady(sched.steady(), B, G)
+    for n in range(1, 5):
+        v = sched.step(n)
+        B, G = scaled_field(p["B"], p["G"], p.get("excitation"), n * p["dt"])
+        st = s.step(v, B, G)
+        exact = s.residual_norm(True, v)
+        assert st["outer"] >= 1                      # at least one double-float residual was used
+        assert abs(st["r"] - exact) <= 0.25 * exact + 5e-15, (n, st["r"], exact)
+    s.close()
