@@ -111,7 +111,7 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                 return xt.v[dk < 0 ? xm : (dk > 0 ? xp : x0)][comp][lj + dj][li + di];
             };
             auto cff = [&](int q, int dk, int dj, int di) -> T { return tc.c[dk < 0 ? prv : cur][q][lj + dj][li + di]; };
-            qms_op_node<T, ADV>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, rY, rZ, rV, xsf, cff, emit);
+            qms_op_node<T, ADV ? 7 : 0>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, rY, rZ, rV, xsf, cff, emit);
         }
         rX += sXk; rY += sYk; rZ += sZk; rV += sZk;
     }

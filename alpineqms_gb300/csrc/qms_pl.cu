@@ -67,7 +67,7 @@ __device__ __forceinline__ T pl_div(T a, T d) {
 // residual in double-float arithmetic, with w the residual of the anchor and x the change of
 // the solution since then).  Partials (optional, FP64 across warps): APPLY / SCALED [0] += y . w
 // (w may be null), [1] += y . y; RESID |r_A|^2, |r_V|^2; none with VCOUPLE.
-template <typename T, bool ADV, int MODE, typename YT = T, typename WT = T>
+template <typename T, int VM, int MODE, typename YT = T, typename WT = T>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap,
          YT* __restrict__ y, const WT* __restrict__ w, double* __restrict__ partials, unsigned* __restrict__ err) {
@@ -165,7 +165,7 @@ qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const
                 return (dk < 0 ? cprv : ccur)[(q * PLCY + lj + dj) * PLX + li + di];
             };
             const bool kfA = k <= 2 || k >= g.Nz - 1, kfZ = k == 1 || k == g.zs;
-            qms_op_node<T, ADV>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, L.comp + rX, 2 * L.comp + rX,
+            qms_op_node<T, VM>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, L.comp + rX, 2 * L.comp + rX,
                                 3 * L.comp + rX, xsf, cff, emit);
         }
         rX += plane;
@@ -313,6 +313,35 @@ __global__ void qk_ref_add_pl(QGrid g, const T* __restrict__ e, const double* __
 
 dim3 qms_node_grid(const QGrid& g) { return dim3((g.Nx + 127) / 128, g.Ny, g.Nz); }
 
+// The velocity components a step uses pick the instantiation: no advection term, one axis, or
+// the general form (FP64 inner vectors: none or general).
+__host__ __forceinline__ bool qms_nonzero(float v) { return v != 0.f; }
+__host__ __forceinline__ bool qms_nonzero(double v) { return v != 0.0; }
+__host__ __forceinline__ bool qms_nonzero(const qdf& v) { return v.h != 0.f || v.l != 0.f; }
+template <typename T>
+static int qms_vel_mask(const QStepPar<T>& P, bool adv, bool axes) {
+    if (!adv) return 0;
+    const int m = (qms_nonzero(P.vx) ? 1 : 0) | (qms_nonzero(P.vy) ? 2 : 0) | (qms_nonzero(P.vz) ? 4 : 0);
+    return axes && (m == 1 || m == 2 || m == 4) ? m : 7;
+}
+
+// STMT with the constant VM set to the mask's instantiation
+#define QMS_WITH_VM(vm, STMT)                                 \
+    switch (vm) {                                             \
+        case 0: { constexpr int VM = 0; STMT; } break;        \
+        case 1: { constexpr int VM = 1; STMT; } break;        \
+        case 2: { constexpr int VM = 2; STMT; } break;        \
+        case 4: { constexpr int VM = 4; STMT; } break;        \
+        default: { constexpr int VM = 7; STMT; } break;       \
+    }
+
+template <typename T, int VM>
+static void op_pl_attrs(int shm) {
+    cudaFuncSetAttribute(qk_op_pl<T, VM, QOPH_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, VM, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, VM, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+}
+
 template <typename T>
 static void op_pl_prepare() {
     static std::atomic<unsigned long long> done{0};
@@ -321,18 +350,18 @@ static void op_pl_prepare() {
     const unsigned long long bit = 1ull << (dev & 63);
     if (done.load(std::memory_order_acquire) & bit) return;
     const int shm = (int)PLTiles<T>::SMEM;
-    cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_op_pl<T, false, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_op_pl<T, true, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    op_pl_attrs<T, 0>(shm);
+    op_pl_attrs<T, 7>(shm);
     if constexpr (sizeof(T) == 4) {
+        op_pl_attrs<T, 1>(shm);
+        op_pl_attrs<T, 2>(shm);
+        op_pl_attrs<T, 4>(shm);
         const int shd = (int)PLTiles<qdf>::SMEM;
-        cudaFuncSetAttribute(qk_op_pl<qdf, false, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             shd);
-        cudaFuncSetAttribute(qk_op_pl<qdf, true, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             shd);
+        cudaFuncSetAttribute(qk_op_pl<qdf, 0, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, shd);
+        cudaFuncSetAttribute(qk_op_pl<qdf, 1, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, shd);
+        cudaFuncSetAttribute(qk_op_pl<qdf, 2, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, shd);
+        cudaFuncSetAttribute(qk_op_pl<qdf, 4, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, shd);
+        cudaFuncSetAttribute(qk_op_pl<qdf, 7, QOPH_RESID, float, qdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, shd);
     }
     done.fetch_or(bit, std::memory_order_acq_rel);
 }
@@ -341,23 +370,30 @@ long long qms_op_pl_num_blocks(const QGrid& g) {
     return (long long)((g.Nx + OTX - 1) / OTX) * ((g.Ny + OTY - 1) / OTY) * ((g.Nz + OKB - 1) / OKB);
 }
 
+template <typename T, int VM>
+static void op_pl_launch(dim3 gs, dim3 bs, size_t shm, cudaStream_t st, int mode, const QGrid& g,
+                         const QStepPar<T>& P, const CUtensorMap& xmap, const CUtensorMap& cmap, T* y, const T* w,
+                         double* partials, unsigned* err) {
+    if constexpr (sizeof(T) == 8 && VM != 0 && VM != 7) {
+        return;                                   // FP64 inner vectors: no or general advection only
+    } else {
+        if (mode == QOPH_APPLY)
+            qk_op_pl<T, VM, QOPH_APPLY><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err);
+        else if (mode == QOPH_VCOUPLE)
+            qk_op_pl<T, VM, QOPH_VCOUPLE><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err);
+        else
+            qk_op_pl<T, VM, QOPH_SCALED><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err);
+    }
+}
+
 template <typename T>
 void qms_launch_op_pl(const QGrid& g, const QStepPar<T>& P, const CUtensorMap& xmap, const CUtensorMap& cmap, bool adv,
                       int mode, T* y, const T* w, double* partials, unsigned* err, cudaStream_t st) {
     op_pl_prepare<T>();
     const dim3 bs(OTX, OTY, 1), gs((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
     const size_t shm = PLTiles<T>::SMEM;
-#define L(ADV, MODE) qk_op_pl<T, ADV, MODE><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err)
-    if (adv) {
-        if (mode == QOPH_APPLY) L(true, QOPH_APPLY);
-        else if (mode == QOPH_VCOUPLE) L(true, QOPH_VCOUPLE);
-        else L(true, QOPH_SCALED);
-    } else {
-        if (mode == QOPH_APPLY) L(false, QOPH_APPLY);
-        else if (mode == QOPH_VCOUPLE) L(false, QOPH_VCOUPLE);
-        else L(false, QOPH_SCALED);
-    }
-#undef L
+    const int vm = qms_vel_mask(P, adv, sizeof(T) == 4);
+    QMS_WITH_VM(vm, (op_pl_launch<T, VM>(gs, bs, shm, st, mode, g, P, xmap, cmap, y, w, partials, err)));
 }
 template void qms_launch_op_pl<float>(const QGrid&, const QStepPar<float>&, const CUtensorMap&, const CUtensorMap&,
                                       bool, int, float*, const float*, double*, unsigned*, cudaStream_t);
@@ -369,8 +405,8 @@ void qms_launch_resid_df(const QGrid& g, const QStepPar<qdf>& P, const CUtensorM
     op_pl_prepare<float>();
     const dim3 bs(OTX, OTY, 1), gs((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
     const size_t shm = PLTiles<qdf>::SMEM;
-    if (adv) qk_op_pl<qdf, true, QOPH_RESID, float, qdf><<<gs, bs, shm, st>>>(g, P, xmap, cmap, r, b, partials, err);
-    else qk_op_pl<qdf, false, QOPH_RESID, float, qdf><<<gs, bs, shm, st>>>(g, P, xmap, cmap, r, b, partials, err);
+    const int vm = qms_vel_mask(P, adv, true);
+    QMS_WITH_VM(vm, (qk_op_pl<qdf, VM, QOPH_RESID, float, qdf><<<gs, bs, shm, st>>>(g, P, xmap, cmap, r, b, partials, err)));
 }
 
 void qms_launch_delta_split(const QGrid& g, const double* x, const double* x0, qdf* dx, double* partials,
