@@ -120,6 +120,7 @@ SIGNATURES = [
     ("qms_get_stats", ctypes.c_int, [_H, ctypes.POINTER(QmsStats)]),
     ("qms_get_fields", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP]),
     ("qms_get_state", ctypes.c_int, [_H, _VP]),
+    ("qms_get_rhs", ctypes.c_int, [_H, _VP]),
     ("qms_set_state", ctypes.c_int, [_H, _VP]),
     ("qms_assemble_csr", ctypes.c_int, [_H, ctypes.c_int, _DP, _DP, _DP, _VP, _VP, _VP, _VP, _VP]),
     ("qms_apply", ctypes.c_int, [_H, ctypes.c_int, _DP, ctypes.c_int, _VP, _VP]),

@@ -184,6 +184,15 @@ int qms_get_state(qms_handle* h, double* x_out) {
     return 0;
 }
 
+int qms_get_rhs(qms_handle* h, double* b_out) {
+    HCHECK(h);
+    if (!b_out) return QMS_ERR_ARG;
+    CKH(cudaSetDevice(h->s.dev));
+    CKH(cudaMemcpyAsync(b_out, h->s.b, h->s.g.n * 8, cudaMemcpyDeviceToHost, h->s.st));
+    CKH(cudaStreamSynchronize(h->s.st));
+    return 0;
+}
+
 int qms_set_state(qms_handle* h, const double* x_in) {
     HCHECK(h);
     if (!x_in) return QMS_ERR_ARG;

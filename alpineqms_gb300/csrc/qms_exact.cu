@@ -331,17 +331,57 @@ __global__ void qk_assemble_csr(QGrid g, const uint8_t* __restrict__ ids, const 
 // K7: right-hand side of the steady (tr = 0) or transient (tr = 1) system.
 // xp is the previous solution (read only when tr = 1).  When `x_dirichlet` is
 // not null the Dirichlet rows of that vector are set to their fixed values, so
-// an iterative solve started from it keeps them exact.
+// an iterative solve started from it keeps them exact.  With `sg` (edge sigma of every A row)
+// and `sdt` (the same divided by dt), both formed by qk_rhs_coef with the same expressions, the
+// transient rows read them instead of forming them again (bit-identical values).
 __global__ void qk_build_rhs(QGrid g, const uint8_t* __restrict__ ids, const QMatTable<double>* __restrict__ tab,
                              Excite e, double dt, int tr, const double* __restrict__ xp, double* __restrict__ b,
-                             double* __restrict__ x_dirichlet) {
+                             double* __restrict__ x_dirichlet, const double* __restrict__ sg,
+                             const double* __restrict__ sdt) {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= g.n) return;
     ExactCoef c{g, ids, tab};
     const double dx = g.dx, dy = g.dy, dz = g.dz;
     double val;
     bool fixed;
-    if (r < g.oY) {
+    if (sg && r < g.oV) {
+        // A rows from the stored sigma / dt
+        long long q = r;
+        int i, j, k;
+        if (r < g.oY) {
+            i = (int)(q % g.xs) + 1; j = (int)((q / g.xs) % g.Ny) + 1; k = (int)(q / ((long long)g.xs * g.Ny)) + 1;
+            fixed = qFixX(g, i, j, k);
+            if (fixed) val = lift_ax(e, (i - 1) * dx, (j - 1) * dy, (k - 1) * dz);
+        } else if (r < g.oZ) {
+            q = r - g.oY;
+            i = (int)(q % g.Nx) + 1; j = (int)((q / g.Nx) % g.ys) + 1; k = (int)(q / ((long long)g.Nx * g.ys)) + 1;
+            fixed = qFixY(g, i, j, k);
+            if (fixed) val = lift_ay(e, (i - 1) * dx, (j - 1) * dy, (k - 1) * dz);
+        } else {
+            q = r - g.oZ;
+            i = (int)(q % g.Nx) + 1; j = (int)((q / g.Nx) % g.Ny) + 1; k = (int)(q / ((long long)g.Nx * g.Ny)) + 1;
+            fixed = qFixZ(g, i, j, k);
+            if (fixed) val = lift_az(e, (i - 1) * dx, (j - 1) * dy, (k - 1) * dz);
+        }
+        if (!fixed) val = tr ? sdt[r] * xp[r] : 0.0;
+    } else if (sg) {
+        // V rows: the divergence of sigma A_prev / dt from the stored edge sigma
+        long long q = r - g.oV;
+        int i = (int)(q % g.Nx) + 1, j = (int)((q / g.Nx) % g.Ny) + 1, k = (int)(q / ((long long)g.Nx * g.Ny)) + 1;
+        fixed = qFixV(g, i, j, k);
+        if (fixed) {
+            val = lift_v(e, (i - 1) * dx, (j - 1) * dy, (k - 1) * dz);
+        } else if (tr) {
+            const long long ax = qAX(g, i, j, k), axm = qAX(g, i - 1, j, k);
+            const long long ay = qAY(g, i, j, k), aym = qAY(g, i, j - 1, k);
+            const long long az = qAZ(g, i, j, k), azm = qAZ(g, i, j, k - 1);
+            val = (sg[ax] * xp[ax] - sg[axm] * xp[axm]) / (dt * dx)
+                + (sg[ay] * xp[ay] - sg[aym] * xp[aym]) / (dt * dy)
+                + (sg[az] * xp[az] - sg[azm] * xp[azm]) / (dt * dz);
+        } else {
+            val = 0.0;
+        }
+    } else if (r < g.oY) {
         long long q = r;
         int i = (int)(q % g.xs) + 1, j = (int)((q / g.xs) % g.Ny) + 1, k = (int)(q / ((long long)g.xs * g.Ny)) + 1;
         fixed = qFixX(g, i, j, k);
@@ -375,6 +415,31 @@ __global__ void qk_build_rhs(QGrid g, const uint8_t* __restrict__ ids, const QMa
     }
     b[r] = val;
     if (x_dirichlet && fixed) x_dirichlet[r] = val;
+}
+
+// Edge sigma of every A row (the expression of F:1465-1476 etc., as ExactCoef forms it) and the
+// same divided by dt: the per-geometry part of the transient right-hand side.
+__global__ void qk_rhs_coef(QGrid g, const uint8_t* __restrict__ ids, const QMatTable<double>* __restrict__ tab,
+                            double dt, double* __restrict__ sg, double* __restrict__ sdt) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.oV) return;
+    ExactCoef c{g, ids, tab};
+    double s;
+    if (r < g.oY) {
+        long long q = r;
+        int i = (int)(q % g.xs) + 1, j = (int)((q / g.xs) % g.Ny) + 1, k = (int)(q / ((long long)g.xs * g.Ny)) + 1;
+        s = c.sgx(i, j, k);
+    } else if (r < g.oZ) {
+        long long q = r - g.oY;
+        int i = (int)(q % g.Nx) + 1, j = (int)((q / g.Nx) % g.ys) + 1, k = (int)(q / ((long long)g.Nx * g.ys)) + 1;
+        s = c.sgy(i, j, k);
+    } else {
+        long long q = r - g.oZ;
+        int i = (int)(q % g.Nx) + 1, j = (int)((q / g.Nx) % g.Ny) + 1, k = (int)(q / ((long long)g.Nx * g.Ny)) + 1;
+        s = c.sgz(i, j, k);
+    }
+    sg[r] = s;
+    sdt[r] = s / dt;
 }
 
 // K8: H at cell centres from the A blocks of x (F:1346-1376); cubes are xs*ys*zs, F-order.
@@ -460,10 +525,18 @@ long long qms_launch_assemble(const QGrid& g, const uint8_t* ids, const QMatTabl
 }
 
 void qms_launch_rhs(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const QmsExcite& ex, double dt,
-                    int tr, const double* xp, double* b, double* x_dirichlet, cudaStream_t st) {
+                    int tr, const double* xp, double* b, double* x_dirichlet, cudaStream_t st, const double* sg,
+                    const double* sdt) {
     int bs = 256;
     long long nb = (g.n + bs - 1) / bs;
-    qk_build_rhs<<<(unsigned)nb, bs, 0, st>>>(g, ids, tab, to_excite(ex), dt, tr, xp, b, x_dirichlet);
+    qk_build_rhs<<<(unsigned)nb, bs, 0, st>>>(g, ids, tab, to_excite(ex), dt, tr, xp, b, x_dirichlet, sg, sdt);
+}
+
+void qms_launch_rhs_coef(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, double dt, double* sg,
+                         double* sdt, cudaStream_t st) {
+    int bs = 256;
+    long long nb = (g.oV + bs - 1) / bs;
+    qk_rhs_coef<<<(unsigned)nb, bs, 0, st>>>(g, ids, tab, dt, sg, sdt);
 }
 
 void qms_launch_hfield(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const double* x, double* Hx,

@@ -13,7 +13,11 @@ long long qms_launch_assemble(const QGrid& g, const uint8_t* ids, const QMatTabl
                               double dt, int tr, const double* xp, long long* ia, int32_t* ja, double* a, double* b,
                               cudaStream_t st);
 void qms_launch_rhs(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const QmsExcite& ex, double dt,
-                    int tr, const double* xp, double* b, double* x_dirichlet, cudaStream_t st);
+                    int tr, const double* xp, double* b, double* x_dirichlet, cudaStream_t st,
+                    const double* sg = nullptr, const double* sdt = nullptr);
+// edge sigma of every A row and sigma / dt (for qms_launch_rhs)
+void qms_launch_rhs_coef(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, double dt, double* sg,
+                         double* sdt, cudaStream_t st);
 void qms_launch_hfield(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const double* x, double* Hx,
                        double* Hy, double* Hz, cudaStream_t st);
 void qms_launch_slice(const QGrid& g, int axis, int index, const double* Hx, const double* Hy, const double* Hz,

@@ -45,7 +45,8 @@ __device__ __forceinline__ T op_div(T a, T d) {
     else return a / d;
 }
 
-template <typename T, bool ADV, int MODE>
+// VM: the velocity components the advection term may use (qms_op_rows.cuh)
+template <typename T, int VM, int MODE>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const T* __restrict__ b,
               T* __restrict__ y, const T* __restrict__ w, double* __restrict__ partials) {
@@ -111,7 +112,7 @@ qk_operator_t(QGrid g, QCoef<T> c, QStepPar<T> P, const T* __restrict__ x, const
                 return xt.v[dk < 0 ? xm : (dk > 0 ? xp : x0)][comp][lj + dj][li + di];
             };
             auto cff = [&](int q, int dk, int dj, int di) -> T { return tc.c[dk < 0 ? prv : cur][q][lj + dj][li + di]; };
-            qms_op_node<T, ADV ? 7 : 0>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, rY, rZ, rV, xsf, cff, emit);
+            qms_op_node<T, VM>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, rY, rZ, rV, xsf, cff, emit);
         }
         rX += sXk; rY += sYk; rZ += sZk; rV += sZk;
     }
@@ -221,12 +222,10 @@ static void qms_operator_prepare() {
     const unsigned long long bit = 1ull << (dev & 63);
     if (done.load(std::memory_order_acquire) & bit) return;
     const int shm = (int)(sizeof(TileCoef<T>) + sizeof(XTile<T>));
-    cudaFuncSetAttribute(qk_operator_t<T, false, QOP_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_operator_t<T, false, QOP_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_operator_t<T, false, QOP_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_operator_t<T, true, QOP_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_operator_t<T, true, QOP_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_operator_t<T, true, QOP_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    for (auto f : {qk_operator_t<T, 0, QOP_APPLY>, qk_operator_t<T, 0, QOP_SCALED>, qk_operator_t<T, 0, QOP_RESID>,
+                   qk_operator_t<T, 7, QOP_APPLY>, qk_operator_t<T, 7, QOP_SCALED>, qk_operator_t<T, 7, QOP_RESID>,
+                   qk_operator_t<T, 1, QOP_RESID>, qk_operator_t<T, 2, QOP_RESID>, qk_operator_t<T, 4, QOP_RESID>})
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
     done.fetch_or(bit, std::memory_order_acq_rel);
 }
 
@@ -236,15 +235,20 @@ void qms_launch_operator(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P
     dim3 bs = opt_block(), gs = opt_grid(g);
     const size_t shm = sizeof(TileCoef<T>) + sizeof(XTile<T>);
     qms_operator_prepare<T>();
-#define L(ADV, MODE) qk_operator_t<T, ADV, MODE><<<gs, bs, shm, st>>>(g, c, P, x, b, y, w, partials)
+#define L(VM, MODE) qk_operator_t<T, VM, MODE><<<gs, bs, shm, st>>>(g, c, P, x, b, y, w, partials)
+    // the residual (the FP64 anchor of every solve) also has one instantiation per velocity axis
+    const int m = (P.vx != T(0) ? 1 : 0) | (P.vy != T(0) ? 2 : 0) | (P.vz != T(0) ? 4 : 0);
     if (adv) {
-        if (mode == QOP_APPLY) L(true, QOP_APPLY);
-        else if (mode == QOP_SCALED) L(true, QOP_SCALED);
-        else L(true, QOP_RESID);
+        if (mode == QOP_APPLY) L(7, QOP_APPLY);
+        else if (mode == QOP_SCALED) L(7, QOP_SCALED);
+        else if (m == 1) L(1, QOP_RESID);
+        else if (m == 2) L(2, QOP_RESID);
+        else if (m == 4) L(4, QOP_RESID);
+        else L(7, QOP_RESID);
     } else {
-        if (mode == QOP_APPLY) L(false, QOP_APPLY);
-        else if (mode == QOP_SCALED) L(false, QOP_SCALED);
-        else L(false, QOP_RESID);
+        if (mode == QOP_APPLY) L(0, QOP_APPLY);
+        else if (mode == QOP_SCALED) L(0, QOP_SCALED);
+        else L(0, QOP_RESID);
     }
 #undef L
 }

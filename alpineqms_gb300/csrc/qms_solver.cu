@@ -475,7 +475,8 @@ void QmsSolver::release() {
     if (gm_scal) cudaFree(gm_scal);
     gm_H = gm_scal = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
-                    status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0};
+                    status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
+                    rsg,   rsdt};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -486,6 +487,7 @@ void QmsSolver::release() {
     ids = nullptr; dtab64 = nullptr; dtab32 = nullptr; x = b = r64 = H = slicebuf = part = S = nullptr;
     status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; mgtmp2 = nullptr; xbest = nullptr;
     xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
+    rsg = rsdt = nullptr;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -566,6 +568,8 @@ int QmsSolver::init(const qms_desc& d) {
         df_resid = true;
         CK(pl_alloc((void**)&xdf, 8));
         CK(pl_alloc((void**)&r0df, 8));
+        CK(cudaMalloc(&rsg, g.oV * 8));
+        CK(cudaMalloc(&rsdt, g.oV * 8));
         CK(cudaMalloc(&x0, n * 8));
         CK(pl_alloc((void**)&rpl, 4));
         CK(cudaMalloc(&ncdf, 6 * qms_pl(g).comp * 8));
@@ -603,7 +607,7 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     // the block-triangular preconditioner's V right-hand side; the double-float residual's x, b,
     // coefficients and FP32 result (mixed precision)
     size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
-    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4) + 6 * qms_pl(g).comp * 8 + g.n * 8;
+    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4) + 6 * qms_pl(g).comp * 8 + g.n * 8 + 2 * g.oV * 8;
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
@@ -638,6 +642,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     qms_launch_node_coef<float>(g, coef32(), nc32, st);
     qms_launch_node_coef<double>(g, coef64(), nc64, st);
     if (df_resid) qms_launch_split_flat(6 * qms_pl(g).comp, nc64, ncdf, st);
+    if (rsg) qms_launch_rhs_coef(g, ids, dtab64, desc.dt, rsg, rsdt, st);
     QCoef<float> c32 = coef32();
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
@@ -1086,7 +1091,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     for (int q = 0; q < 3; q++) { ex.B[q] = B[q]; ex.v[q] = v[q]; }
     for (int q = 0; q < 9; q++) ex.G[q] = G[q];
     // b from the previous solution (x); Dirichlet values written into x (warm start keeps them exact)
-    qms_launch_rhs(g, ids, dtab64, ex, desc.dt, transient ? 1 : 0, x, b, x, st);
+    qms_launch_rhs(g, ids, dtab64, ex, desc.dt, transient ? 1 : 0, x, b, x, st, rsg, rsdt);
     anchor_ready = false;          // the first residual of this solve is the FP64 anchor
     nlaunch++;
     CK(cudaMemsetAsync(status, 0, 4, st));

@@ -55,6 +55,8 @@ struct QmsSolver {
     bool df_resid = false;
     bool anchor_ready = false;
     double* x0 = nullptr;
+    double* rsg = nullptr;      // edge sigma of every A row, and / dt (transient right-hand side)
+    double* rsdt = nullptr;
     qdf* xdf = nullptr;         // x - x0
     qdf* r0df = nullptr;
     qdf* ncdf = nullptr;

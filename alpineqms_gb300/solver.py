@@ -106,6 +106,11 @@ class QMSSolver:
         check(self.L.qms_get_state(self.h, x.ctypes.data), self.h, "qms_get_state")
         return x
 
+    def get_rhs(self) -> np.ndarray:
+        x = np.empty(self.n, np.float64)
+        check(self.L.qms_get_rhs(self.h, x.ctypes.data), self.h, "qms_get_rhs")
+        return x
+
     def set_state(self, x: np.ndarray):
         x = np.ascontiguousarray(x, dtype=np.float64)
         assert x.size == self.n

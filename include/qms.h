@@ -145,6 +145,9 @@ int qms_get_stats(const qms_handle* h, qms_stats* out);
  * index), each in the record layout of F:1380-1394. */
 int qms_get_fields(qms_handle* h, int which, int axis, int index, double* out);
 int qms_get_state(qms_handle* h, double* x_out);          /* n_dims doubles */
+int qms_get_rhs(qms_handle* h, double* b_out);            /* n_dims doubles: the right-hand side of the last
+                                                             solve (RHS of F:1457-2191, Dirichlet values
+                                                             in their rows) */
 int qms_set_state(qms_handle* h, const double* x_in);
 
 /* Verification path: CSR of the steady (transient = 0) or transient system and

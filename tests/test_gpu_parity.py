@@ -352,3 +352,24 @@ def test_double_float_residual_agrees_with_fp64():
         assert st["outer"] >= 1                      # at least one double-float residual was used
         assert abs(st["r"] - exact) <= 0.25 * exact + 5e-15, (n, st["r"], exact)
     s.close()
+
+
+@pytest.mark.gpu
+def test_transient_rhs_bit_exact():
+    """The solver's transient right-hand side (K7 with the per-geometry edge sigma and sigma / dt
+    stored once) equals the oracle's assembled RHS bit for bit."""
+    xs, ys, zs = 10, 9, 11
+    geom, props, d = make_case(xs, ys, zs, seed=5)
+    dt = 1e-5
+    c = o.materials(xs, ys, zs, geom, props)
+    n = o.sizes(xs, ys, zs)[0]
+    x = np.random.default_rng(7).standard_normal(n) * 1e-3
+    v, B = (1.5, -0.5, 0.25), (2e-3, -1e-3, 5e-3)
+    G = np.array([0.05, 0.02, -0.01, 0.02, -0.03, 0.04, -0.01, 0.04, -0.02])
+    s = solver_for(xs, ys, zs, d, dt, geom, props)
+    s.set_state(x)
+    s.step(v, B, G)
+    b = s.get_rhs()
+    s.close()
+    _, _, _, br = o.assemble(xs, ys, zs, *d, c, True, dt, v, B, G, x_prev=x)
+    assert np.array_equal(b, br)
