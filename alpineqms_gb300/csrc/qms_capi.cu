@@ -68,6 +68,7 @@ int qms_create(const qms_desc* d, qms_handle** out) {
     if (dd.check_every <= 0) dd.check_every = 1;
     if (!(dd.mg_alpha > 0)) dd.mg_alpha = 1.0;
     if (dd.mg_coarse_sweeps < 0) dd.mg_coarse_sweeps = 0;
+    if (dd.mg_v_sweeps < 0) dd.mg_v_sweeps = 0;
     if (dd.max_inner <= 0 || dd.max_outer < 0 || !(dd.tol > 0) || !(dd.inner_rtol > 0) || dd.mg_sweeps < 1 ||
         !(dd.mg_omega > 0)) {
         std::lock_guard<std::mutex> lk(g_err_mu);

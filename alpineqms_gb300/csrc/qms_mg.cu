@@ -825,6 +825,8 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     const long long* dmo = dmoff + (QS == 2 ? 3 : 0);                    // their dense coarsest inverses
     const int nl = (int)lv.size();
     const int mv = (QS == 0 && mask_v) ? 1 : 0;
+    // sweeps on each side: the V-block cycle may use its own count
+    const int n1 = (QS == 2 && nu_v > 0) ? nu_v : nu1, n2 = (QS == 2 && nu_v > 0) ? nu_v : nu2;
     const int sc = scaled ? 1 : 0;
     mg0_prepare<T>();
     struct Buf { T* p; const CUtensorMap* m; };
@@ -837,10 +839,10 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     // level 0: nu1 + nu2 sweeps alternate between x0 and t0 (the prolongation is in place);
     // start in t0 when that count is even so that the last write lands in x0
     Buf x{x0, &x0map}, t{t0, &t0map};
-    if ((nu1 + nu2) % 2 == 0) std::swap(x, t);
+    if ((n1 + n2) % 2 == 0) std::swap(x, t);
     MG0(0, x, x.p, nullptr);
     launches++;
-    for (int s = 1; s < nu1; s++) {
+    for (int s = 1; s < n1; s++) {
         MG0(1, x, t.p, nullptr);
         std::swap(x, t);
         launches++;
@@ -848,7 +850,8 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     MG0(2, x, nullptr, lv[1].b);
     launches++;
     // levels >= 1: nu_coarse sweeps on each side when set
-    const int nuc1 = nu_coarse > 0 ? nu_coarse : nu1, nuc2 = nu_coarse > 0 ? nu_coarse : nu2;
+    const int nuc1 = (QS == 2 && nu_v > 0) ? nu_v : (nu_coarse > 0 ? nu_coarse : nu1);
+    const int nuc2 = (QS == 2 && nu_v > 0) ? nu_v : (nu_coarse > 0 ? nu_coarse : nu2);
     for (int l = 1; l < nl; l++) {
         MGLevelDev<T>& L = lv[l];
         if (l == nl - 1) {
@@ -886,7 +889,7 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     }
     mg0_prolong<T, QS><<<dim3((g0.Nx + 127) / 128, g0.Ny, g0.Nz), 128, 0, st>>>(g0, mv, x.p, lv[1], lv[1].x, alpha);
     launches++;
-    for (int s = 0; s < nu2; s++) {
+    for (int s = 0; s < n2; s++) {
         MG0(1, x, t.p, nullptr);
         std::swap(x, t);
         launches++;

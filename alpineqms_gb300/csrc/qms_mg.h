@@ -38,6 +38,7 @@ struct QmsMG {
     long long* dmoff = nullptr;
     int nu1 = 2, nu2 = 2;
     int nu_coarse = 0;             // sweeps on each side on levels >= 1 (0: nu1 / nu2)
+    int nu_v = 0;                  // sweeps on each side, every level, of a V-block cycle (0: as above)
     T omega = T(0.8);
     T alpha = T(1);
     int min_coarse = 5;

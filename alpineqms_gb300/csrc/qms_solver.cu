@@ -655,12 +655,14 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
                 QmsMG<double>& M = mgd[tr];
                 M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = desc.mg_omega; M.alpha = desc.mg_alpha;
                 M.nu_coarse = desc.mg_coarse_sweeps;
+                M.nu_v = desc.mg_v_sweeps;
                 rc = M.build(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, tr == 1), vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             } else {
                 QmsMG<float>& M = mgf[tr];
                 M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = (float)desc.mg_omega; M.alpha = (float)desc.mg_alpha;
                 M.nu_coarse = desc.mg_coarse_sweeps;
+                M.nu_v = desc.mg_v_sweeps;
                 rc = M.build(g, coef32(), qms_step_par<float>(g, 0, 0, 0, desc.dt, tr == 1), (float)vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             }

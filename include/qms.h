@@ -104,6 +104,8 @@ typedef struct {
                                 residual the A correction leaves in the V rows; 0 block-diagonal */
     int mg_coarse_sweeps;    /* Jacobi sweeps before and after the coarse correction on levels >= 1
                                 (0: mg_sweeps) */
+    int mg_v_sweeps;         /* sweeps on each side, on every level, of the block-triangular
+                                preconditioner's V-block cycle (0: as the A blocks) */
 } qms_desc;
 
 typedef struct {
