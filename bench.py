@@ -402,6 +402,13 @@ def run_gpu(args):
                 "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
                 "config": {"workload": "moving_plate_256", "grid": [inp.xs, inp.ys, inp.zs], "dof": n,
                            "dt": inp.dt, "precision": args.precision, "tol": desc.tol,
+                           "solver": {"krylov": "fgmres" if desc.krylov == 0 else "bicgstab",
+                                      "gmres_m": desc.gmres_m, "mg_sweeps": desc.mg_sweeps,
+                                      "mg_omega": desc.mg_omega, "mg_alpha": desc.mg_alpha,
+                                      "mg_coupling": "lower block-triangular" if desc.mg_coupling == 1
+                                      else "block-diagonal",
+                                      "residual": "FP64 anchor + double-float" if args.precision == "mixed"
+                                      else "FP64"},
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                            "l2": "inputs larger than L2 (one FP32 vector = %.0f MB)" % (n * 4 / 1e6)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": prof["launches"],
