@@ -40,7 +40,8 @@ class QmsDesc(ctypes.Structure):
                 ("gmres_m", ctypes.c_int),
                 ("use_graphs", ctypes.c_int), ("mg_region_cut", ctypes.c_double),
                 ("mg_alpha", ctypes.c_double), ("mg_coupling", ctypes.c_int),
-                ("mg_coarse_sweeps", ctypes.c_int), ("mg_v_sweeps", ctypes.c_int)]
+                ("mg_coarse_sweeps", ctypes.c_int), ("mg_v_sweeps", ctypes.c_int),
+                ("mg_tail_points", ctypes.c_int)]
 
 
 class QmsStats(ctypes.Structure):

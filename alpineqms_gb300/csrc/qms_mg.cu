@@ -282,6 +282,122 @@ __global__ void mg_dense(MGLevelDev<T> L, const double* __restrict__ minv, const
 }
 
 
+// ------------------------------------------------------------------ coarse tail
+// The last levels of a cycle (a few thousand points per block at most) in one launch: one CTA
+// per block runs their whole V-cycle for that block, passes separated by __syncthreads, the
+// data L2-resident.  These levels otherwise cost a launch per sweep, most of it latency.
+#define MG_TAIL_MAX_LEVELS 8
+template <typename T>
+struct MGTail {
+    int nl;                                     // tail levels; the last is the coarsest
+    MGLevelDev<T> L[MG_TAIL_MAX_LEVELS];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(1024) mg_tail(MGTail<T> tl, const double* __restrict__ minv,
+                                                const long long* __restrict__ moff, T omega, T alpha, int nu1,
+                                                int nu2, int mask_v) {
+    const int b = blockIdx.x;
+    const int nb = tl.L[0].nb;
+    const bool masked = mask_v && b == nb - 1;
+    T* xcur[MG_TAIL_MAX_LEVELS];
+    T* tcur[MG_TAIL_MAX_LEVELS];
+    auto npts = [&](const MGBlockDesc& B) { return (long long)B.n1 * B.n2 * B.n3; };
+    // x_out = x_in + omega D^-1 (b - A x_in) over the block's points
+    auto sweep = [&](const MGLevelDev<T>& L, const T* xin, T* xout) {
+        const MGBlockDesc& B = L.blk[b];
+        const long long n = npts(B);
+        for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+            const long long t = B.off + q;
+            const T di = masked ? T(0) : L.dinv[t];
+            if (di == T(0)) { xout[t] = T(0); continue; }
+            const int i = (int)(q % B.n1), j = (int)((q / B.n1) % B.n2), k = (int)(q / ((long long)B.n1 * B.n2));
+            xout[t] = xin[t] + omega * di * (L.b[t] - apply7(L, B, t, i, j, k, xin));
+        }
+        __syncthreads();
+    };
+    const int last = tl.nl - 1;
+    for (int l = 0; l < last; l++) {
+        const MGLevelDev<T>& L = tl.L[l];
+        const MGBlockDesc& B = L.blk[b];
+        const long long n = npts(B);
+        T* x = L.x;
+        T* t = L.t;
+        for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+            const long long p = B.off + q;
+            x[p] = masked ? T(0) : omega * L.dinv[p] * L.b[p];
+        }
+        __syncthreads();
+        for (int s = 1; s < nu1; s++) {
+            sweep(L, x, t);
+            T* w = x; x = t; t = w;
+        }
+        xcur[l] = x;
+        tcur[l] = t;
+        // residual summed over each 2x2x2 aggregate -> the next level's right-hand side
+        const MGLevelDev<T>& C = tl.L[l + 1];
+        const MGBlockDesc& cb = C.blk[b];
+        const long long nc = npts(cb);
+        for (long long q = threadIdx.x; q < nc; q += blockDim.x) {
+            const int I = (int)(q % cb.n1), J = (int)((q / cb.n1) % cb.n2), K = (int)(q / ((long long)cb.n1 * cb.n2));
+            T acc = T(0);
+            if (!masked)
+                for (int dk = 0; dk < 2; dk++) for (int dj = 0; dj < 2; dj++) for (int dd = 0; dd < 2; dd++) {
+                    const int i = 2 * I + dd, j = 2 * J + dj, k = 2 * K + dk;
+                    if (i >= B.n1 || j >= B.n2 || k >= B.n3) continue;
+                    const long long f = B.off + i + (long long)j * B.n1 + (long long)k * B.n1 * B.n2;
+                    if (L.dinv[f] == T(0)) continue;
+                    acc += L.b[f] - apply7(L, B, f, i, j, k, x);
+                }
+            C.b[cb.off + q] = acc;
+        }
+        __syncthreads();
+    }
+    {   // coarsest: x = Minv b (FP64 dense; pseudo-inverse for V)
+        const MGLevelDev<T>& C = tl.L[last];
+        const MGBlockDesc& B = C.blk[b];
+        const int m = (int)npts(B);
+        const double* M = minv + moff[b];
+        for (int r = threadIdx.x; r < m; r += blockDim.x) {
+            double acc = 0.0;
+            if (!masked)
+                for (int c = 0; c < m; c++) acc += M[(long long)r * m + c] * (double)C.b[B.off + c];
+            C.x[B.off + r] = (T)acc;
+        }
+        xcur[last] = C.x;
+        __syncthreads();
+    }
+    for (int l = last - 1; l >= 0; l--) {
+        const MGLevelDev<T>& L = tl.L[l];
+        const MGLevelDev<T>& C = tl.L[l + 1];
+        const MGBlockDesc& B = L.blk[b];
+        const MGBlockDesc& cb = C.blk[b];
+        const long long n = npts(B);
+        T* x = xcur[l];
+        T* t = tcur[l];
+        const T* xc = xcur[l + 1];
+        for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+            const long long p = B.off + q;
+            if (L.dinv[p] == T(0) || masked) { x[p] = T(0); continue; }
+            const int i = (int)(q % B.n1), j = (int)((q / B.n1) % B.n2), k = (int)(q / ((long long)B.n1 * B.n2));
+            x[p] += alpha * xc[cb.off + (i >> 1) + (long long)(j >> 1) * cb.n1 + (long long)(k >> 1) * cb.n1 * cb.n2];
+        }
+        __syncthreads();
+        for (int s = 0; s < nu2; s++) {
+            sweep(L, x, t);
+            T* w = x; x = t; t = w;
+        }
+        xcur[l] = x;
+    }
+    // the level above reads the tail's top level from its x array
+    const MGLevelDev<T>& L0 = tl.L[0];
+    if (xcur[0] != L0.x) {
+        const MGBlockDesc& B = L0.blk[b];
+        const long long n = npts(B);
+        for (long long q = threadIdx.x; q < n; q += blockDim.x) L0.x[B.off + q] = xcur[0][B.off + q];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Level-0 kernels on node tiles.  Level 0 of every block is the global unknown
 // vector itself, and its 7-point operators are the self couplings of the rows
@@ -852,8 +968,26 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     // levels >= 1: nu_coarse sweeps on each side when set
     const int nuc1 = (QS == 2 && nu_v > 0) ? nu_v : (nu_coarse > 0 ? nu_coarse : nu1);
     const int nuc2 = (QS == 2 && nu_v > 0) ? nu_v : (nu_coarse > 0 ? nu_coarse : nu2);
+    // coarse tail: from level lt on, every level has at most tail_points points per block and
+    // the whole sub-cycle runs as one launch (one CTA per block)
+    auto maxpts = [](const MGLevelDev<T>& L) {
+        long long m = 0;
+        for (int q = 0; q < L.nb; q++) m = std::max(m, (long long)L.blk[q].n1 * L.blk[q].n2 * L.blk[q].n3);
+        return m;
+    };
+    int lt = nl - 1;
+    if (tail_points > 0)
+        while (lt > 1 && maxpts(lv[lt - 1]) <= tail_points && nl - (lt - 1) <= MG_TAIL_MAX_LEVELS) lt--;
     for (int l = 1; l < nl; l++) {
         MGLevelDev<T>& L = lv[l];
+        if (l == lt && tail_points > 0) {
+            MGTail<T> tl{};
+            tl.nl = nl - lt;
+            for (int q = 0; q < tl.nl; q++) tl.L[q] = lv[lt + q];
+            mg_tail<T><<<L.nb, 1024, 0, st>>>(tl, dminv, dmo, omega, alpha, nuc1, nuc2, mv);
+            launches++;
+            break;
+        }
         if (l == nl - 1) {
             mg_dense<<<L.nb, 256, 0, st>>>(L, dminv, dmo, L.b, L.x, mv);
             launches++;
@@ -873,7 +1007,7 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
         mg_restrict<<<nblk(lv[l + 1].total), 256, 0, st>>>(L, L.b, nullptr, xl, lv[l + 1], lv[l + 1].b, mv);
         launches++;
     }
-    for (int l = nl - 2; l >= 1; l--) {
+    for (int l = lt - 1; l >= 1; l--) {
         MGLevelDev<T>& L = lv[l];
         T* xl = L.x;
         T* tl = L.t;

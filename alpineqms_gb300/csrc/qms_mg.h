@@ -39,6 +39,7 @@ struct QmsMG {
     int nu1 = 2, nu2 = 2;
     int nu_coarse = 0;             // sweeps on each side on levels >= 1 (0: nu1 / nu2)
     int nu_v = 0;                  // sweeps on each side, every level, of a V-block cycle (0: as above)
+    long long tail_points = 4096;  // levels of at most this many points per block run as one launch (0: off)
     T omega = T(0.8);
     T alpha = T(1);
     int min_coarse = 5;

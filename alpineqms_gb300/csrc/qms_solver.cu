@@ -656,6 +656,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
                 M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = desc.mg_omega; M.alpha = desc.mg_alpha;
                 M.nu_coarse = desc.mg_coarse_sweeps;
                 M.nu_v = desc.mg_v_sweeps;
+                M.tail_points = desc.mg_tail_points == 0 ? 4096 : std::max(0, desc.mg_tail_points);
                 rc = M.build(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, tr == 1), vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             } else {
@@ -663,6 +664,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
                 M.nu1 = M.nu2 = desc.mg_sweeps; M.omega = (float)desc.mg_omega; M.alpha = (float)desc.mg_alpha;
                 M.nu_coarse = desc.mg_coarse_sweeps;
                 M.nu_v = desc.mg_v_sweeps;
+                M.tail_points = desc.mg_tail_points == 0 ? 4096 : std::max(0, desc.mg_tail_points);
                 rc = M.build(g, coef32(), qms_step_par<float>(g, 0, 0, 0, desc.dt, tr == 1), (float)vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             }

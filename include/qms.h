@@ -106,6 +106,8 @@ typedef struct {
                                 (0: mg_sweeps) */
     int mg_v_sweeps;         /* sweeps on each side, on every level, of the block-triangular
                                 preconditioner's V-block cycle (0: as the A blocks) */
+    int mg_tail_points;      /* the coarse levels with at most this many points per block run their
+                                sub-cycle as one launch, one CTA per block (0: 4096; < 0: off) */
 } qms_desc;
 
 typedef struct {
