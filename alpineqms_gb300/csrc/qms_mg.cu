@@ -23,6 +23,7 @@
 // back and processed by one launch through a packed block-descriptor table.
 // Smoother: weighted Jacobi.  Coarsest level: dense FP64 inverse per block.
 #include "qms_mg.h"
+#include "qms_pl.h"
 #include "qms_tile.cuh"
 
 #include <atomic>
@@ -612,8 +613,9 @@ template <typename T, int QS>
 __global__ void mg0_prolong(QGrid g, int mask_v, T* __restrict__ x, MGLevelDev<T> C, const T* __restrict__ xc,
                             T alpha) {
     using S = MG0Set<QS>;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > g.Nx) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
     const int I = (i - 1) >> 1, J = (j - 1) >> 1, K = (k - 1) >> 1;
     auto coarse = [&](int q) {
         const MGBlockDesc& cb = C.blk[q - S::Q0];
@@ -1021,7 +1023,7 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
         L.x = xl;
         L.t = tl;
     }
-    mg0_prolong<T, QS><<<dim3((g0.Nx + 127) / 128, g0.Ny, g0.Nz), 128, 0, st>>>(g0, mv, x.p, lv[1], lv[1].x, alpha);
+    mg0_prolong<T, QS><<<qms_node_grid(g0), qms_node_block(), 0, st>>>(g0, mv, x.p, lv[1], lv[1].x, alpha);
     launches++;
     for (int s = 0; s < n2; s++) {
         MG0(1, x, t.p, nullptr);

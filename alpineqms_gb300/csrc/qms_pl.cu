@@ -213,8 +213,9 @@ __global__ void __launch_bounds__(256) qk_delta_split(QGrid g, const double* __r
 // when given
 __global__ void qk_split_ref_pl(QGrid g, const double* __restrict__ src, qdf* __restrict__ dst,
                                 float* __restrict__ hi) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > g.Nx) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
     const QPL L = qms_pl(g);
     const long long t = qms_pl_node(g, L, i, j, k);
     auto one = [&](long long ref, long long pl) {
@@ -244,8 +245,9 @@ __global__ void qk_pl_scale(long long n, const float* __restrict__ r, const doub
 
 // FP32 diagonal of the operator in the padded layout (Dirichlet rows 1)
 __global__ void qk_diag_pl(QGrid g, QCoef<float> c, QStepPar<float> P, float* __restrict__ dg) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > g.Nx) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
     const QPL L = qms_pl(g);
     const long long t = qms_pl_node(g, L, i, j, k);
     if (i <= g.xs) {
@@ -283,8 +285,9 @@ __global__ void qk_diag_pl(QGrid g, QCoef<float> c, QStepPar<float> P, float* __
 template <typename T>
 __global__ void qk_pl_from_ref(QGrid g, const double* __restrict__ r64, const double* __restrict__ scale,
                                T* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > g.Nx) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
     const QPL L = qms_pl(g);
     const long long t = qms_pl_node(g, L, i, j, k);
     const double s = scale ? scale[0] : 1.0;
@@ -298,8 +301,9 @@ __global__ void qk_pl_from_ref(QGrid g, const double* __restrict__ r64, const do
 template <typename T>
 __global__ void qk_ref_add_pl(QGrid g, const T* __restrict__ e, const double* __restrict__ scale,
                               double* __restrict__ x) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > g.Nx) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
     const QPL L = qms_pl(g);
     const long long t = qms_pl_node(g, L, i, j, k);
     const double s = scale[0];
@@ -311,7 +315,10 @@ __global__ void qk_ref_add_pl(QGrid g, const T* __restrict__ e, const double* __
 
 }  // namespace
 
-dim3 qms_node_grid(const QGrid& g) { return dim3((g.Nx + 127) / 128, g.Ny, g.Nz); }
+dim3 qms_node_grid(const QGrid& g) {
+    return dim3((g.Nx + QMS_NODE_BX - 1) / QMS_NODE_BX, (g.Ny + QMS_NODE_BY - 1) / QMS_NODE_BY, g.Nz);
+}
+dim3 qms_node_block() { return dim3(QMS_NODE_BX, QMS_NODE_BY, 1); }
 
 // The velocity components a step uses pick the instantiation: no advection term, one axis, or
 // the general form (FP64 inner vectors: none or general).
@@ -415,7 +422,7 @@ void qms_launch_delta_split(const QGrid& g, const double* x, const double* x0, q
 }
 
 void qms_launch_split_ref_pl(const QGrid& g, const double* src, qdf* dst, float* hi, cudaStream_t st) {
-    qk_split_ref_pl<<<qms_node_grid(g), 128, 0, st>>>(g, src, dst, hi);
+    qk_split_ref_pl<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, src, dst, hi);
 }
 
 void qms_launch_split_flat(long long n, const double* src, qdf* dst, cudaStream_t st) {
@@ -428,19 +435,19 @@ void qms_launch_pl_scale(long long n, const float* r, const double* scale, float
 
 void qms_launch_diag_pl(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st) {
     cudaMemsetAsync(dg, 0, qms_pl(g).n * sizeof(float), st);
-    qk_diag_pl<<<qms_node_grid(g), 128, 0, st>>>(g, c, P, dg);
+    qk_diag_pl<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, c, P, dg);
 }
 
 template <typename T>
 void qms_launch_pl_from_ref(const QGrid& g, const double* r64, const double* scale, T* out, cudaStream_t st) {
-    qk_pl_from_ref<T><<<qms_node_grid(g), 128, 0, st>>>(g, r64, scale, out);
+    qk_pl_from_ref<T><<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, r64, scale, out);
 }
 template void qms_launch_pl_from_ref<float>(const QGrid&, const double*, const double*, float*, cudaStream_t);
 template void qms_launch_pl_from_ref<double>(const QGrid&, const double*, const double*, double*, cudaStream_t);
 
 template <typename T>
 void qms_launch_ref_add_pl(const QGrid& g, const T* e, const double* scale, double* x, cudaStream_t st) {
-    qk_ref_add_pl<T><<<qms_node_grid(g), 128, 0, st>>>(g, e, scale, x);
+    qk_ref_add_pl<T><<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, e, scale, x);
 }
 template void qms_launch_ref_add_pl<float>(const QGrid&, const float*, const double*, double*, cudaStream_t);
 template void qms_launch_ref_add_pl<double>(const QGrid&, const double*, const double*, double*, cudaStream_t);

@@ -4,7 +4,11 @@
 #include "qms_tma.cuh"
 #include "qms_df.cuh"
 
-dim3 qms_node_grid(const QGrid& g);                 // one thread per node: (ceil(Nx/128), Ny, Nz) x 128
+// one thread per node: blocks of QMS_NODE_BX (along x) x QMS_NODE_BY (along y) nodes of a plane
+#define QMS_NODE_BX 32
+#define QMS_NODE_BY 16
+dim3 qms_node_grid(const QGrid& g);
+dim3 qms_node_block();
 long long qms_op_pl_num_blocks(const QGrid& g);
 
 // y = M x (mode QOPH_APPLY) or D^-1 M x (QOPH_SCALED) on padded vectors; x and the node

@@ -375,10 +375,11 @@ __global__ void qk_gm_solve(int k, int m, const double* __restrict__ Hm, double*
 // x[ref] += nrm * sum_i y_i Z_i[PL]   (FP64 accumulation of the refinement); one thread per
 // node, its (up to) four unknowns
 template <typename T, int NV>
-__global__ void __launch_bounds__(128) qk_gm_update(QGrid g, int m, GmPtrs Z, const double* __restrict__ Gm,
+__global__ void __launch_bounds__(QMS_NODE_BX * QMS_NODE_BY) qk_gm_update(QGrid g, int m, GmPtrs Z, const double* __restrict__ Gm,
                                                     const double* __restrict__ S, double* __restrict__ x) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > g.Nx) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
     const double* yv = Gm + 8 + 3 * m + 1;
     T y[NV];
     const T* zp[NV];
@@ -424,7 +425,7 @@ template <typename T>
 static void gm_update(int nv, cudaStream_t st, const QGrid& g, int m, const GmPtrs& Z, const double* Gm,
                       const double* S, double* x) {
     switch (nv) {
-#define C(N) case N: qk_gm_update<T, N><<<qms_node_grid(g), 128, 0, st>>>(g, m, Z, Gm, S, x); break;
+#define C(N) case N: qk_gm_update<T, N><<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, m, Z, Gm, S, x); break;
         GM_CASES(C)
 #undef C
     }
@@ -627,6 +628,8 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     gm_k_seen = 0;
     gm_lrate[0] = gm_lrate[1] = 0.0;
     gm_k_fine = false;
+    gm_k_floor = 0;
+    gm_k_floor_age = 0;
     if (nmat < 0 || nmat > QMS_MAX_SLOTS - 1) { err = "nmat must be in 0..255"; return QMS_ERR_ARG; }
     const long long ncell = (long long)g.xs * g.ys * g.zs;
     if (host_slots) {
@@ -1225,12 +1228,18 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // probe downwards after every solve that two replays brought below tol / 3 (in steps of a
     // fifth of k until the first solve that needed a third replay, one step after that), and
     // step back up by two when a solve needed a third
+    // A count that needed a third replay is not probed again for 32 solves.
     if (graph_cycles > 0 && rel <= desc.tol) {
         if (graph_cycles >= 3) {
+            gm_k_floor = gm_k_est + 1;
+            gm_k_floor_age = 0;
             gm_k_est = std::min(gm_m, gm_k_est + 2);
             gm_k_fine = true;
-        } else if (graph_cycles == 2 && gm_cycles == 2 && rel < desc.tol / 3.0) {
-            gm_k_est = std::max(6, gm_k_est - (gm_k_fine ? 1 : std::max(1, gm_k_est / 5)));
+        } else if (graph_cycles == 2 && gm_cycles == 2) {
+            if (gm_k_floor > 0 && ++gm_k_floor_age >= 32) { gm_k_floor--; gm_k_floor_age = 0; }
+            if (rel < desc.tol / 3.0)
+                gm_k_est = std::max(std::max(6, gm_k_floor),
+                                    gm_k_est - (gm_k_fine ? 1 : std::max(1, gm_k_est / 5)));
         }
     }
     unsigned stt = 0;

@@ -142,6 +142,8 @@ struct QmsSolver {
     int gm_k_est = 0;           // FGMRES iterations replayed per refinement iteration (0: not yet known)
     int gm_k_seen = 0;          // largest count seen while running with host checks
     bool gm_k_fine = false;     // gm_k_est has overshot downwards once: tune it in single steps
+    int gm_k_floor = 0;         // smallest count not yet known to need a third replay
+    int gm_k_floor_age = 0;     // solves since gm_k_floor was set or lowered
     // log of the per-iteration residual reduction of FGMRES, smoothed over solves: [0] the first
     // cycle of a solve, [1] the later ones (which start from a residual rich in slow modes)
     double gm_lrate[2] = {0, 0};
