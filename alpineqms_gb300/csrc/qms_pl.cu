@@ -70,7 +70,8 @@ __device__ __forceinline__ T pl_div(T a, T d) {
 template <typename T, int VM, int MODE, typename YT = T, typename WT = T>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap,
-         YT* __restrict__ y, const WT* __restrict__ w, double* __restrict__ partials, unsigned* __restrict__ err) {
+         YT* __restrict__ y, const WT* __restrict__ w, double* __restrict__ partials, unsigned* __restrict__ err,
+         WT* __restrict__ yfull = nullptr) {
     using TL = PLTiles<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][4][PLXY][PLX]
@@ -124,6 +125,7 @@ qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const
         if constexpr (MODE == QOPH_RESID) {
             const T out = w[row] - acc / diag;
             y[row] = out.h;
+            if (yfull) yfull[row] = out;          // the residual in full, for the next solve's anchor
             if (partials) {
                 const float o = out.h;
                 if (is_a) red0 += o * o;
@@ -207,6 +209,62 @@ __global__ void __launch_bounds__(256) qk_delta_split(QGrid g, const double* __r
     if (threadIdx.x == 0) partials[2 * (long long)gridDim.x + blockIdx.x] = sa;
     const double sv = qBlockSum(xv, sh);
     if (threadIdx.x == 0) partials[3 * (long long)gridDim.x + blockIdx.x] = sv;
+}
+
+// 1 / diag M (transient form), formed in FP64 like the rows' own diagonal, as double-float
+__global__ void qk_dinv_df(QGrid g, QCoef<double> c, QStepPar<double> P, qdf* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
+    const QPL L = qms_pl(g);
+    const long long t = qms_pl_node(g, L, i, j, k);
+    if (i <= g.xs) {
+        double d = 1.0;
+        if (!qFixX(g, i, j, k))
+            d = (c.imuz(i, j, k) + c.imuz(i, j - 1, k)) * P.idy2 + (c.imuy(i, j, k) + c.imuy(i, j, k - 1)) * P.idz2 +
+                (c.imux(i, j, k) + c.imux(i - 1, j, k)) * P.idx2 + c.sgx(i, j, k) * P.idt;
+        out[t] = qdf_split(1.0 / d);
+    }
+    if (j <= g.ys) {
+        double d = 1.0;
+        if (!qFixY(g, i, j, k))
+            d = (c.imuz(i, j, k) + c.imuz(i - 1, j, k)) * P.idx2 + (c.imux(i, j, k) + c.imux(i, j, k - 1)) * P.idz2 +
+                (c.imuy(i, j, k) + c.imuy(i, j - 1, k)) * P.idy2 + c.sgy(i, j, k) * P.idt;
+        out[L.comp + t] = qdf_split(1.0 / d);
+    }
+    if (k <= g.zs) {
+        double d = 1.0;
+        if (!qFixZ(g, i, j, k))
+            d = (c.imuy(i, j, k) + c.imuy(i - 1, j, k)) * P.idx2 + (c.imux(i, j, k) + c.imux(i, j - 1, k)) * P.idy2 +
+                (c.imuz(i, j, k) + c.imuz(i, j, k - 1)) * P.idz2 + c.sgz(i, j, k) * P.idt;
+        out[2 * L.comp + t] = qdf_split(1.0 / d);
+    }
+    double d = 1.0;
+    if (!qFixV(g, i, j, k)) {
+        const double f = P.sigfloor;
+        d = (fmax(c.sgx(i, j, k), f) + fmax(c.sgx(i - 1, j, k), f)) * P.idx2 +
+            (fmax(c.sgy(i, j, k), f) + fmax(c.sgy(i, j - 1, k), f)) * P.idy2 +
+            (fmax(c.sgz(i, j, k), f) + fmax(c.sgz(i, j, k - 1), f)) * P.idz2;
+    }
+    out[3 * L.comp + t] = qdf_split(1.0 / d);
+}
+
+// r0 = rprev + D^-1 (b - bprev): the residual of the previous solution against the new
+// right-hand side, from the previous solve's final residual (the operator is unchanged)
+__global__ void qk_chain_anchor(QGrid g, const qdf* __restrict__ rprev, const double* __restrict__ b,
+                                const double* __restrict__ bprev, const qdf* __restrict__ dinv, qdf* __restrict__ r0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
+    const QPL L = qms_pl(g);
+    const long long t = qms_pl_node(g, L, i, j, k);
+    auto one = [&](long long ref, long long pl) {
+        r0[pl] = rprev[pl] + qdf_split(b[ref] - bprev[ref]) * dinv[pl];
+    };
+    if (i <= g.xs) one(qAX(g, i, j, k), t);
+    if (j <= g.ys) one(qAY(g, i, j, k), L.comp + t);
+    if (k <= g.zs) one(qAZ(g, i, j, k), 2 * L.comp + t);
+    one(qV(g, i, j, k), 3 * L.comp + t);
 }
 
 // double -> double-float, reference unknown order -> padded layout; its high words also to hi
@@ -408,12 +466,14 @@ template void qms_launch_op_pl<double>(const QGrid&, const QStepPar<double>&, co
                                        bool, int, double*, const double*, double*, unsigned*, cudaStream_t);
 
 void qms_launch_resid_df(const QGrid& g, const QStepPar<qdf>& P, const CUtensorMap& xmap, const CUtensorMap& cmap,
-                         bool adv, float* r, const qdf* b, double* partials, unsigned* err, cudaStream_t st) {
+                         bool adv, float* r, const qdf* b, double* partials, unsigned* err, cudaStream_t st,
+                         qdf* rfull) {
     op_pl_prepare<float>();
     const dim3 bs(OTX, OTY, 1), gs((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
     const size_t shm = PLTiles<qdf>::SMEM;
     const int vm = qms_vel_mask(P, adv, true);
-    QMS_WITH_VM(vm, (qk_op_pl<qdf, VM, QOPH_RESID, float, qdf><<<gs, bs, shm, st>>>(g, P, xmap, cmap, r, b, partials, err)));
+    QMS_WITH_VM(vm, (qk_op_pl<qdf, VM, QOPH_RESID, float, qdf><<<gs, bs, shm, st>>>(g, P, xmap, cmap, r, b, partials, err,
+                                                                                   rfull)));
 }
 
 void qms_launch_delta_split(const QGrid& g, const double* x, const double* x0, qdf* dx, double* partials,
@@ -427,6 +487,15 @@ void qms_launch_split_ref_pl(const QGrid& g, const double* src, qdf* dst, float*
 
 void qms_launch_split_flat(long long n, const double* src, qdf* dst, cudaStream_t st) {
     qk_split_flat<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 16), 256, 0, st>>>(n, src, dst);
+}
+
+void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st) {
+    qk_dinv_df<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, c, P, out);
+}
+
+void qms_launch_chain_anchor(const QGrid& g, const qdf* rprev, const double* b, const double* bprev, const qdf* dinv,
+                             qdf* r0, cudaStream_t st) {
+    qk_chain_anchor<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, rprev, b, bprev, dinv, r0);
 }
 
 void qms_launch_pl_scale(long long n, const float* r, const double* scale, float* out, cudaStream_t st) {

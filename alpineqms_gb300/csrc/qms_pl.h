@@ -20,8 +20,15 @@ void qms_launch_op_pl(const QGrid& g, const QStepPar<T>& P, const CUtensorMap& x
 // refinement residual in double-float from an anchor: r = (float) (r0 - D^-1 M dx) on padded
 // vectors, with r0 the anchor's scaled residual and dx (xmap) the change of x since the anchor,
 // both double-float, and the node coefficients (cmap) as double-float; partials |r_A|^2, |r_V|^2
+// rfull (optional): the residual itself, double-float
 void qms_launch_resid_df(const QGrid& g, const QStepPar<qdf>& P, const CUtensorMap& xmap, const CUtensorMap& cmap,
-                         bool adv, float* r, const qdf* r0, double* partials, unsigned* err, cudaStream_t st);
+                         bool adv, float* r, const qdf* r0, double* partials, unsigned* err, cudaStream_t st,
+                         qdf* rfull = nullptr);
+// 1 / diag M as double-float (padded layout)
+void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st);
+// r0 = rprev + D^-1 (b - bprev)   (b, bprev in reference order; the rest padded, double-float)
+void qms_launch_chain_anchor(const QGrid& g, const qdf* rprev, const double* b, const double* bprev, const qdf* dinv,
+                             qdf* r0, cudaStream_t st);
 // dx = x - x0 as double-float (padded layout) and the partials |x_A|^2, |x_V|^2 of nb blocks
 void qms_launch_delta_split(const QGrid& g, const double* x, const double* x0, qdf* dx, double* partials,
                             long long nb, cudaStream_t st);

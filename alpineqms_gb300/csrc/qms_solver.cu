@@ -477,7 +477,7 @@ void QmsSolver::release() {
     gm_H = gm_scal = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
                     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
-                    rsg,   rsdt};
+                    rsg,   rsdt,   bprev,     rfin,  dinvdf};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -489,6 +489,7 @@ void QmsSolver::release() {
     status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; mgtmp2 = nullptr; xbest = nullptr;
     xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
     rsg = rsdt = nullptr;
+    bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -571,6 +572,9 @@ int QmsSolver::init(const qms_desc& d) {
         CK(pl_alloc((void**)&r0df, 8));
         CK(cudaMalloc(&rsg, g.oV * 8));
         CK(cudaMalloc(&rsdt, g.oV * 8));
+        CK(cudaMalloc(&bprev, n * 8));
+        CK(pl_alloc((void**)&rfin, 8));
+        CK(pl_alloc((void**)&dinvdf, 8));
         CK(cudaMalloc(&x0, n * 8));
         CK(pl_alloc((void**)&rpl, 4));
         CK(cudaMalloc(&ncdf, 6 * qms_pl(g).comp * 8));
@@ -608,7 +612,7 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     // the block-triangular preconditioner's V right-hand side; the double-float residual's x, b,
     // coefficients and FP32 result (mixed precision)
     size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
-    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4) + 6 * qms_pl(g).comp * 8 + g.n * 8 + 2 * g.oV * 8;
+    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4 + 8 + 8) + 6 * qms_pl(g).comp * 8 + 2 * g.n * 8 + 2 * g.oV * 8;
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
@@ -646,6 +650,8 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     qms_launch_node_coef<double>(g, coef64(), nc64, st);
     if (df_resid) qms_launch_split_flat(6 * qms_pl(g).comp, nc64, ncdf, st);
     if (rsg) qms_launch_rhs_coef(g, ids, dtab64, desc.dt, rsg, rsdt, st);
+    if (dinvdf) qms_launch_dinv_df(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, true), dinvdf, st);
+    rfin_ok = false;
     QCoef<float> c32 = coef32();
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
@@ -978,9 +984,10 @@ void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], boo
         OpEv* ev = prof_begin(3, (double)g.n * 8 * 4 + (double)g.xs * g.ys * g.zs);
         qms_launch_delta_split(g, x, x0, xdf, part, nbop, st);
         qms_launch_resid_df(g, qms_step_par<qdf>(g, v[0], v[1], v[2], desc.dt, transient), xdfmap, cdfmap, adv, rpl,
-                            r0df, part, status, st);
+                            r0df, part, status, st, rfin);
         nlaunch += 2;
         prof_end(ev);
+        last_resid_df = true;
     } else {
         QStepPar<double> P = qms_step_par<double>(g, v[0], v[1], v[2], desc.dt, transient);
         op<double>(adv, QOPH_RESID, P, x, b, r64, nullptr, part);
@@ -991,6 +998,7 @@ void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], boo
             nlaunch++;
             anchor_ready = true;
         }
+        last_resid_df = false;
     }
     finalize(FIN_RESID, 4, nbop);
 }
@@ -1097,10 +1105,26 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     QmsExcite ex;
     for (int q = 0; q < 3; q++) { ex.B[q] = B[q]; ex.v[q] = v[q]; }
     for (int q = 0; q < 9; q++) ex.G[q] = G[q];
+    // the previous solve's final residual anchors this one when the operator is the same
+    const bool chain = df_resid && transient && rfin_ok && chain_len < 16 && chain_v[0] == v[0] &&
+                       chain_v[1] == v[1] && chain_v[2] == v[2];
+    if (chain) {
+        CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));   // the previous solution
+        std::swap(b, bprev);
+    }
     // b from the previous solution (x); Dirichlet values written into x (warm start keeps them exact)
     qms_launch_rhs(g, ids, dtab64, ex, desc.dt, transient ? 1 : 0, x, b, x, st, rsg, rsdt);
-    anchor_ready = false;          // the first residual of this solve is the FP64 anchor
     nlaunch++;
+    anchor_ready = false;          // the first residual of this solve is the FP64 anchor ...
+    if (chain) {                   // ... unless it follows from the previous one
+        qms_launch_chain_anchor(g, rfin, b, bprev, dinvdf, r0df, st);
+        nlaunch++;
+        anchor_ready = true;
+        chain_len++;
+    } else {
+        chain_len = 0;
+    }
+    rfin_ok = false;
     CK(cudaMemsetAsync(status, 0, 4, st));
     const bool adv = v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
     const bool use_cg = !transient && !adv;
@@ -1214,7 +1238,12 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         stats.inner_iterations += it;
         outer++;
     }
+    // the final residual (rfin) anchors the next transient solve when it belongs to the state
+    // that this solve leaves in x
+    rfin_ok = df_resid && transient && last_resid_df && rel <= desc.tol;
+    for (int q = 0; q < 3; q++) chain_v[q] = v[q];
     if (!(rel <= desc.tol) && best_rel < rel && std::isfinite(best_rel)) {
+        rfin_ok = false;
         CK(cudaMemcpyAsync(x, xbest, g.n * 8, cudaMemcpyDeviceToDevice, st));
         rel = best_rel;
         if (rel <= desc.tol) stats.status &= ~(unsigned)QMS_ST_NO_CONVERGENCE;

@@ -55,6 +55,16 @@ struct QmsSolver {
     bool df_resid = false;
     bool anchor_ready = false;
     double* x0 = nullptr;
+    // Chained anchor: a transient solve with the operator of the previous one starts from that
+    // solve's final residual, r0 = r_fin + D^-1 (b - b_prev), instead of an FP64 residual (an
+    // exact one every 16 steps, and whenever the operator or the state changed otherwise).
+    double* bprev = nullptr;    // right-hand side of the previous solve
+    qdf* rfin = nullptr;        // the last double-float residual, in full
+    qdf* dinvdf = nullptr;      // 1 / diag M of the transient operator
+    bool rfin_ok = false;       // rfin is the final residual of the state in x, for chain_v
+    bool last_resid_df = false;
+    int chain_len = 0;
+    double chain_v[3] = {0, 0, 0};
     double* rsg = nullptr;      // edge sigma of every A row, and / dt (transient right-hand side)
     double* rsdt = nullptr;
     qdf* xdf = nullptr;         // x - x0
