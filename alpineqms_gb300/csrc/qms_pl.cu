@@ -267,6 +267,41 @@ __global__ void qk_chain_anchor(QGrid g, const qdf* __restrict__ rprev, const do
     one(qV(g, i, j, k), 3 * L.comp + t);
 }
 
+// The residual is the anchor itself (x is the anchor state): r = r0 into rfloat (FP32) and rfull,
+// with the partials |r_A|^2, |r_V|^2, |x_A|^2, |x_V|^2 of gridDim.x (= nb) blocks
+__global__ void __launch_bounds__(256) qk_anchor_resid(QGrid g, const qdf* __restrict__ r0, const double* __restrict__ x,
+                                                       float* __restrict__ rfloat, qdf* __restrict__ rfull,
+                                                       double* __restrict__ partials) {
+    const QPL L = qms_pl(g);
+    float ra = 0.f, rv = 0.f, xa = 0.f, xv = 0.f;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.Nn; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.Nx) + 1, j = (int)((t / g.Nx) % g.Ny) + 1, k = (int)(t / ((long long)g.Nx * g.Ny)) + 1;
+        const long long nd = qms_pl_node(g, L, i, j, k);
+        auto one = [&](long long ref, long long pl, float& racc, float& xacc) {
+            const qdf r = r0[pl];
+            rfloat[pl] = r.h;
+            rfull[pl] = r;
+            racc += r.h * r.h;
+            const float f = qdf_split(x[ref]).h;
+            xacc += f * f;
+        };
+        if (i <= g.xs) one(qAX(g, i, j, k), nd, ra, xa);
+        if (j <= g.ys) one(qAY(g, i, j, k), L.comp + nd, ra, xa);
+        if (k <= g.zs) one(qAZ(g, i, j, k), 2 * L.comp + nd, ra, xa);
+        one(qV(g, i, j, k), 3 * L.comp + nd, rv, xv);
+    }
+    __shared__ double sh[32];
+    const long long nb = gridDim.x;
+    double s = qBlockSum(ra, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    s = qBlockSum(rv, sh);
+    if (threadIdx.x == 0) partials[nb + blockIdx.x] = s;
+    s = qBlockSum(xa, sh);
+    if (threadIdx.x == 0) partials[2 * nb + blockIdx.x] = s;
+    s = qBlockSum(xv, sh);
+    if (threadIdx.x == 0) partials[3 * nb + blockIdx.x] = s;
+}
+
 // double -> double-float, reference unknown order -> padded layout; its high words also to hi
 // when given
 __global__ void qk_split_ref_pl(QGrid g, const double* __restrict__ src, qdf* __restrict__ dst,
@@ -487,6 +522,11 @@ void qms_launch_split_ref_pl(const QGrid& g, const double* src, qdf* dst, float*
 
 void qms_launch_split_flat(long long n, const double* src, qdf* dst, cudaStream_t st) {
     qk_split_flat<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 16), 256, 0, st>>>(n, src, dst);
+}
+
+void qms_launch_anchor_resid(const QGrid& g, const qdf* r0, const double* x, float* rfloat, qdf* rfull,
+                             double* partials, long long nb, cudaStream_t st) {
+    qk_anchor_resid<<<(unsigned)nb, 256, 0, st>>>(g, r0, x, rfloat, rfull, partials);
 }
 
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st) {

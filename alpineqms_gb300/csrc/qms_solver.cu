@@ -978,7 +978,15 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
 }
 
 void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], bool exact) {
-    if (df_resid && anchor_ready && !exact) {
+    if (df_resid && anchor_ready && anchor_is_residual && !exact) {
+        // x is the anchor state: the residual is the anchor's
+        OpEv* ev = prof_begin(3, (double)g.n * 8 * 3);
+        qms_launch_anchor_resid(g, r0df, x, rpl, rfin, part, nbop, st);
+        nlaunch++;
+        prof_end(ev);
+        anchor_is_residual = false;
+        last_resid_df = true;
+    } else if (df_resid && anchor_ready && !exact) {
         // double-float from the anchor: dx = x - x0 split into the padded layout (with the |x|^2
         // partials), then the TMA-staged stencil on the FP32 pipe
         OpEv* ev = prof_begin(3, (double)g.n * 8 * 4 + (double)g.xs * g.ys * g.zs);
@@ -1116,11 +1124,17 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     qms_launch_rhs(g, ids, dtab64, ex, desc.dt, transient ? 1 : 0, x, b, x, st, rsg, rsdt);
     nlaunch++;
     anchor_ready = false;          // the first residual of this solve is the FP64 anchor ...
+    anchor_is_residual = false;
     if (chain) {                   // ... unless it follows from the previous one
         qms_launch_chain_anchor(g, rfin, b, bprev, dinvdf, r0df, st);
         nlaunch++;
         anchor_ready = true;
         chain_len++;
+        // same field: the Dirichlet values did not move, x is the anchor state
+        bool same = true;
+        for (int q = 0; q < 3; q++) same = same && chain_B[q] == B[q];
+        for (int q = 0; q < 9; q++) same = same && chain_G[q] == G[q];
+        anchor_is_residual = same;
     } else {
         chain_len = 0;
     }
@@ -1241,7 +1255,8 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // the final residual (rfin) anchors the next transient solve when it belongs to the state
     // that this solve leaves in x
     rfin_ok = df_resid && transient && last_resid_df && rel <= desc.tol;
-    for (int q = 0; q < 3; q++) chain_v[q] = v[q];
+    for (int q = 0; q < 3; q++) { chain_v[q] = v[q]; chain_B[q] = B[q]; }
+    for (int q = 0; q < 9; q++) chain_G[q] = G[q];
     if (!(rel <= desc.tol) && best_rel < rel && std::isfinite(best_rel)) {
         rfin_ok = false;
         CK(cudaMemcpyAsync(x, xbest, g.n * 8, cudaMemcpyDeviceToDevice, st));
