@@ -72,7 +72,11 @@ __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB :
 qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap,
          YT* __restrict__ y, const WT* __restrict__ w, double* __restrict__ partials, unsigned* __restrict__ err,
          WT* __restrict__ yfull = nullptr) {
-    using TL = PLTiles<T>;
+    // VCOUPLE reads only what the V rows' A couplings need: the three A blocks of x (xmap over
+    // them) and the three conductivities (cmap over them)
+    constexpr bool VC = MODE == QOPH_VCOUPLE;
+    constexpr int C0 = VC ? 3 : 0;
+    using TL = PLTiles<T, VC ? 3 : 4, VC ? 3 : 6>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][4][PLXY][PLX]
     T* csm = xsm + 4 * TL::XSLOT;                             // [3 slots][6][PLCY][PLX]
@@ -164,7 +168,8 @@ qk_op_pl(QGrid g, QStepPar<T> P, const __grid_constant__ CUtensorMap xmap, const
                 return b[(comp * PLXY + lj + dj) * PLX + li + di];
             };
             auto cff = [&](int q, int dk, int dj, int di) -> T {
-                return (dk < 0 ? cprv : ccur)[(q * PLCY + lj + dj) * PLX + li + di];
+                if (VC && q < C0) return T(0);     // read by the A rows only, which VCOUPLE drops
+                return (dk < 0 ? cprv : ccur)[((q - C0) * PLCY + lj + dj) * PLX + li + di];
             };
             const bool kfA = k <= 2 || k >= g.Nz - 1, kfZ = k == 1 || k == g.zs;
             qms_op_node<T, VM>(g, P, i, j, k, fijX, fijY, fijZ, kfA, kfZ, rX, L.comp + rX, 2 * L.comp + rX,
@@ -439,7 +444,8 @@ template <typename T, int VM>
 static void op_pl_attrs(int shm) {
     cudaFuncSetAttribute(qk_op_pl<T, VM, QOPH_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
     cudaFuncSetAttribute(qk_op_pl<T, VM, QOPH_SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
-    cudaFuncSetAttribute(qk_op_pl<T, VM, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm);
+    cudaFuncSetAttribute(qk_op_pl<T, VM, QOPH_VCOUPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)PLTiles<T, 3, 3>::SMEM);
 }
 
 template <typename T>
@@ -480,7 +486,8 @@ static void op_pl_launch(dim3 gs, dim3 bs, size_t shm, cudaStream_t st, int mode
         if (mode == QOPH_APPLY)
             qk_op_pl<T, VM, QOPH_APPLY><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err);
         else if (mode == QOPH_VCOUPLE)
-            qk_op_pl<T, VM, QOPH_VCOUPLE><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err);
+            qk_op_pl<T, VM, QOPH_VCOUPLE><<<gs, bs, PLTiles<T, 3, 3>::SMEM, st>>>(g, P, xmap, cmap, y, w, partials,
+                                                                                    err);
         else
             qk_op_pl<T, VM, QOPH_SCALED><<<gs, bs, shm, st>>>(g, P, xmap, cmap, y, w, partials, err);
     }

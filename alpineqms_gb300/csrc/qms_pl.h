@@ -12,7 +12,8 @@ dim3 qms_node_block();
 long long qms_op_pl_num_blocks(const QGrid& g);
 
 // y = M x (mode QOPH_APPLY) or D^-1 M x (QOPH_SCALED) on padded vectors; x and the node
-// coefficients come through their tensor maps (qms_make_pl_map, 10 and 9 rows per box)
+// coefficients come through their tensor maps (qms_make_pl_map, 10 and 9 rows per box).
+// QOPH_VCOUPLE takes the maps of x's three A blocks and of the three conductivities.
 template <typename T>
 void qms_launch_op_pl(const QGrid& g, const QStepPar<T>& P, const CUtensorMap& xmap, const CUtensorMap& cmap, bool adv,
                       int mode, T* y, const T* w, double* partials, unsigned* err, cudaStream_t st);

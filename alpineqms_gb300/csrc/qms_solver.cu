@@ -823,7 +823,8 @@ void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool
             // the A correction leaves in the V rows (row-scaled like r)
             T* tv = (T*)mgtmp2;
             cycle(r, 1, cm);
-            qms_launch_op_pl<T>(g, *P, tmap(z), cm, adv, QOPH_VCOUPLE, tv, r, nullptr, status, st);
+            qms_launch_op_pl<T>(g, *P, tmapq(z, 1), f32 ? cmapV32 : cmapV64, adv, QOPH_VCOUPLE, tv, r, nullptr,
+                                status, st);
             cycle(tv, 2, f32 ? cmapV32 : cmapV64);
             nlaunch++;
             regions.apply<T>(tv, bscale, z, st, nlaunch);
