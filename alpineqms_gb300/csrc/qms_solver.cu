@@ -477,7 +477,7 @@ void QmsSolver::release() {
     gm_H = gm_scal = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
                     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
-                    rsg,   rsdt,   bprev,     rfin,  dinvdf};
+                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -489,7 +489,7 @@ void QmsSolver::release() {
     status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; mgtmp2 = nullptr; xbest = nullptr;
     xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
     rsg = rsdt = nullptr;
-    bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0;
+    bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0; xold = nullptr;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -573,6 +573,7 @@ int QmsSolver::init(const qms_desc& d) {
         CK(cudaMalloc(&rsg, g.oV * 8));
         CK(cudaMalloc(&rsdt, g.oV * 8));
         CK(cudaMalloc(&bprev, n * 8));
+        CK(cudaMalloc(&xold, n * 8));
         CK(pl_alloc((void**)&rfin, 8));
         CK(pl_alloc((void**)&dinvdf, 8));
         CK(cudaMalloc(&x0, n * 8));
@@ -1117,7 +1118,11 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // the previous solve's final residual anchors this one when the operator is the same
     const bool chain = df_resid && transient && rfin_ok && chain_len < 16 && chain_v[0] == v[0] &&
                        chain_v[1] == v[1] && chain_v[2] == v[2];
+    // a chained solve after a chained solve: x0 still holds the solution before the previous one
+    const bool extrap = chain && chain_len >= 1 && desc.extrapolate;
     if (chain) {
+        // copies, not pointer swaps: the captured refinement graphs hold these addresses
+        if (extrap) CK(cudaMemcpyAsync(xold, x0, g.n * 8, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));   // the previous solution
         std::swap(b, bprev);
     }
@@ -1136,6 +1141,13 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         for (int q = 0; q < 3; q++) same = same && chain_B[q] == B[q];
         for (int q = 0; q < 9; q++) same = same && chain_G[q] == G[q];
         anchor_is_residual = same;
+        if (extrap) {
+            // start from the linear extrapolation of the last two states (Dirichlet rows keep the
+            // values just written); the first residual then follows incrementally from the anchor
+            qms_launch_extrapolate(g, x, xold, st);
+            nlaunch++;
+            anchor_is_residual = false;
+        }
     } else {
         chain_len = 0;
     }
@@ -1273,18 +1285,22 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // probe downwards after every solve that two replays brought below tol / 3 (in steps of a
     // fifth of k until the first solve that needed a third replay, one step after that), and
     // step back up by two when a solve needed a third
-    // A count that needed a third replay is not probed again for 32 solves.
+    // A count that needed a third replay is not probed again for 32 solves.  (One longer cycle
+    // in place of two does not pay: the FP32 inner solve stalls within a cycle, and a single
+    // cycle needed ~23 steps where two of 7 sufficed.)
     if (graph_cycles > 0 && rel <= desc.tol) {
+        if (gm_k_floor > 0 && ++gm_k_floor_age >= 32) { gm_k_floor--; gm_k_floor_age = 0; }
         if (graph_cycles >= 3) {
             gm_k_floor = gm_k_est + 1;
             gm_k_floor_age = 0;
             gm_k_est = std::min(gm_m, gm_k_est + 2);
             gm_k_fine = true;
         } else if (graph_cycles == 2 && gm_cycles == 2) {
-            if (gm_k_floor > 0 && ++gm_k_floor_age >= 32) { gm_k_floor--; gm_k_floor_age = 0; }
             if (rel < desc.tol / 3.0)
                 gm_k_est = std::max(std::max(6, gm_k_floor),
                                     gm_k_est - (gm_k_fine ? 1 : std::max(1, gm_k_est / 5)));
+        } else if (graph_cycles == 1 && gm_cycles == 1 && rel < desc.tol / 3.0) {
+            gm_k_est = std::max(std::max(6, gm_k_floor), gm_k_est - 1);
         }
     }
     unsigned stt = 0;
