@@ -51,7 +51,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->mg_region_cut = 0.0;
     d->mg_alpha = 1.5;
     d->mg_coupling = 1;
-    d->extrapolate = 1;
+    d->extrapolate = 2;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }

@@ -254,13 +254,17 @@ __global__ void qk_dinv_df(QGrid g, QCoef<double> c, QStepPar<double> P, qdf* __
     out[3 * L.comp + t] = qdf_split(1.0 / d);
 }
 
-// x = x + (x - xold) on the rows that are not Dirichlet rows: the linear extrapolation of the
-// state from the last two steps, the start of the next solve
-__global__ void qk_extrapolate(QGrid g, double* __restrict__ x, const double* __restrict__ xold) {
+// The extrapolation of the state from the last steps on the rows that are not Dirichlet rows,
+// the start of the next solve: x = 2 x - xold (linear), or with xold2 (the step before)
+// x = 3 x - 3 xold + xold2 (quadratic)
+__global__ void qk_extrapolate(QGrid g, double* __restrict__ x, const double* __restrict__ xold,
+                               const double* __restrict__ xold2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.Nx || j > g.Ny) return;
-    auto one = [&](long long r) { x[r] = 2.0 * x[r] - xold[r]; };
+    auto one = [&](long long r) {
+        x[r] = xold2 ? 3.0 * (x[r] - xold[r]) + xold2[r] : 2.0 * x[r] - xold[r];
+    };
     if (i <= g.xs && !qFixX(g, i, j, k)) one(qAX(g, i, j, k));
     if (j <= g.ys && !qFixY(g, i, j, k)) one(qAY(g, i, j, k));
     if (k <= g.zs && !qFixZ(g, i, j, k)) one(qAZ(g, i, j, k));
@@ -549,8 +553,8 @@ void qms_launch_anchor_resid(const QGrid& g, const qdf* r0, const double* x, flo
     qk_anchor_resid<<<(unsigned)nb, 256, 0, st>>>(g, r0, x, rfloat, rfull, partials);
 }
 
-void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, cudaStream_t st) {
-    qk_extrapolate<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, x, xold);
+void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const double* xold2, cudaStream_t st) {
+    qk_extrapolate<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, x, xold, xold2);
 }
 
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st) {

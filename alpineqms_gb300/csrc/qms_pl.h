@@ -28,8 +28,8 @@ void qms_launch_resid_df(const QGrid& g, const QStepPar<qdf>& P, const CUtensorM
 // the residual when x is the anchor state: rfloat = (float) r0, rfull = r0, the four partials of nb blocks
 void qms_launch_anchor_resid(const QGrid& g, const qdf* r0, const double* x, float* rfloat, qdf* rfull,
                              double* partials, long long nb, cudaStream_t st);
-// x = 2 x - xold on the non-Dirichlet rows (reference order)
-void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, cudaStream_t st);
+// x = 2 x - xold, or with xold2 3 x - 3 xold + xold2, on the non-Dirichlet rows (reference order)
+void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const double* xold2, cudaStream_t st);
 // 1 / diag M as double-float (padded layout)
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st);
 // r0 = rprev + D^-1 (b - bprev)   (b, bprev in reference order; the rest padded, double-float)

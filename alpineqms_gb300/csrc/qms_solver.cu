@@ -477,7 +477,7 @@ void QmsSolver::release() {
     gm_H = gm_scal = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
                     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
-                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold};
+                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -489,7 +489,7 @@ void QmsSolver::release() {
     status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; mgtmp2 = nullptr; xbest = nullptr;
     xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
     rsg = rsdt = nullptr;
-    bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0; xold = nullptr;
+    bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0; xold = xold2 = nullptr;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -574,6 +574,7 @@ int QmsSolver::init(const qms_desc& d) {
         CK(cudaMalloc(&rsdt, g.oV * 8));
         CK(cudaMalloc(&bprev, n * 8));
         CK(cudaMalloc(&xold, n * 8));
+        if (d.extrapolate >= 2) CK(cudaMalloc(&xold2, n * 8));
         CK(pl_alloc((void**)&rfin, 8));
         CK(pl_alloc((void**)&dinvdf, 8));
         CK(cudaMalloc(&x0, n * 8));
@@ -1120,8 +1121,10 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
                        chain_v[1] == v[1] && chain_v[2] == v[2];
     // a chained solve after a chained solve: x0 still holds the solution before the previous one
     const bool extrap = chain && chain_len >= 1 && desc.extrapolate;
+    const bool quad = extrap && chain_len >= 2 && xold2;
     if (chain) {
         // copies, not pointer swaps: the captured refinement graphs hold these addresses
+        if (xold2) CK(cudaMemcpyAsync(xold2, xold, g.n * 8, cudaMemcpyDeviceToDevice, st));
         if (extrap) CK(cudaMemcpyAsync(xold, x0, g.n * 8, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));   // the previous solution
         std::swap(b, bprev);
@@ -1144,7 +1147,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         if (extrap) {
             // start from the linear extrapolation of the last two states (Dirichlet rows keep the
             // values just written); the first residual then follows incrementally from the anchor
-            qms_launch_extrapolate(g, x, xold, st);
+            qms_launch_extrapolate(g, x, xold, quad ? xold2 : nullptr, st);
             nlaunch++;
             anchor_is_residual = false;
         }

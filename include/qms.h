@@ -108,9 +108,10 @@ typedef struct {
                                 preconditioner's V-block cycle (0: as the A blocks) */
     int mg_tail_points;      /* the coarse levels with at most this many points per block run their
                                 sub-cycle as one launch, one CTA per block (0: 4096; < 0: off) */
-    int extrapolate;         /* 1 (default): a transient step that follows two steps with the same
-                                operator starts from the linear extrapolation 2 x_n - x_(n-1) of
-                                the last two solutions instead of x_n; 0: from x_n */
+    int extrapolate;         /* a transient step that follows steps with the same operator starts
+                                from an extrapolation of the last solutions instead of x_n:
+                                2 (default) quadratic once three are known, 3 x_n - 3 x_(n-1) +
+                                x_(n-2) (linear before); 1 linear, 2 x_n - x_(n-1); 0 none */
 } qms_desc;
 
 typedef struct {
