@@ -9,6 +9,7 @@
 //   qk_slice         K8  2-D slice of the H cubes        F:1380-1394, F:2276-2290
 //   qk_ids_from_geom K9  float64 IDs -> uint8 slots      F:234-254
 #include "qms_internal.h"
+#include "qms_pl.h"
 
 namespace {
 
@@ -417,6 +418,55 @@ __global__ void qk_build_rhs(QGrid g, const uint8_t* __restrict__ ids, const QMa
     if (x_dirichlet && fixed) x_dirichlet[r] = val;
 }
 
+// The same right-hand side with the stored edge sigma, one thread per node (its up to four rows):
+// the same expressions as qk_build_rhs's stored-sigma path, without per-row index divisions.
+__global__ void qk_build_rhs_nodes(QGrid g, Excite e, double dt, int tr, const double* __restrict__ xp,
+                                   double* __restrict__ b, double* __restrict__ x_dirichlet,
+                                   const double* __restrict__ sg, const double* __restrict__ sdt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
+    const double dx = g.dx, dy = g.dy, dz = g.dz;
+    const double xq = (i - 1) * dx, yq = (j - 1) * dy, zq = (k - 1) * dz;
+    auto put = [&](long long r, bool fixed, double val) {
+        b[r] = val;
+        if (x_dirichlet && fixed) x_dirichlet[r] = val;
+    };
+    if (i <= g.xs) {
+        const long long r = qAX(g, i, j, k);
+        const bool fixed = qFixX(g, i, j, k);
+        put(r, fixed, fixed ? lift_ax(e, xq, yq, zq) : (tr ? sdt[r] * xp[r] : 0.0));
+    }
+    if (j <= g.ys) {
+        const long long r = qAY(g, i, j, k);
+        const bool fixed = qFixY(g, i, j, k);
+        put(r, fixed, fixed ? lift_ay(e, xq, yq, zq) : (tr ? sdt[r] * xp[r] : 0.0));
+    }
+    if (k <= g.zs) {
+        const long long r = qAZ(g, i, j, k);
+        const bool fixed = qFixZ(g, i, j, k);
+        put(r, fixed, fixed ? lift_az(e, xq, yq, zq) : (tr ? sdt[r] * xp[r] : 0.0));
+    }
+    {
+        const long long r = qV(g, i, j, k);
+        const bool fixed = qFixV(g, i, j, k);
+        double val;
+        if (fixed) {
+            val = lift_v(e, xq, yq, zq);
+        } else if (tr) {
+            const long long ax = qAX(g, i, j, k), axm = qAX(g, i - 1, j, k);
+            const long long ay = qAY(g, i, j, k), aym = qAY(g, i, j - 1, k);
+            const long long az = qAZ(g, i, j, k), azm = qAZ(g, i, j, k - 1);
+            val = (sg[ax] * xp[ax] - sg[axm] * xp[axm]) / (dt * dx)
+                + (sg[ay] * xp[ay] - sg[aym] * xp[aym]) / (dt * dy)
+                + (sg[az] * xp[az] - sg[azm] * xp[azm]) / (dt * dz);
+        } else {
+            val = 0.0;
+        }
+        put(r, fixed, val);
+    }
+}
+
 // Edge sigma of every A row (the expression of F:1465-1476 etc., as ExactCoef forms it) and the
 // same divided by dt: the per-geometry part of the transient right-hand side.
 __global__ void qk_rhs_coef(QGrid g, const uint8_t* __restrict__ ids, const QMatTable<double>* __restrict__ tab,
@@ -527,6 +577,11 @@ long long qms_launch_assemble(const QGrid& g, const uint8_t* ids, const QMatTabl
 void qms_launch_rhs(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const QmsExcite& ex, double dt,
                     int tr, const double* xp, double* b, double* x_dirichlet, cudaStream_t st, const double* sg,
                     const double* sdt) {
+    if (sg) {
+        qk_build_rhs_nodes<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, to_excite(ex), dt, tr, xp, b, x_dirichlet,
+                                                                           sg, sdt);
+        return;
+    }
     int bs = 256;
     long long nb = (g.n + bs - 1) / bs;
     qk_build_rhs<<<(unsigned)nb, bs, 0, st>>>(g, ids, tab, to_excite(ex), dt, tr, xp, b, x_dirichlet, sg, sdt);

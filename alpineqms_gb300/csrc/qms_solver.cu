@@ -1123,8 +1123,9 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     const bool extrap = chain && chain_len >= 1 && desc.extrapolate;
     const bool quad = extrap && chain_len >= 2 && xold2;
     if (chain) {
-        // copies, not pointer swaps: the captured refinement graphs hold these addresses
-        if (xold2) CK(cudaMemcpyAsync(xold2, xold, g.n * 8, cudaMemcpyDeviceToDevice, st));
+        // x0 is copied, not swapped: the captured refinement graphs hold its address (xold and
+        // xold2 are read by the extrapolation only)
+        if (xold2) std::swap(xold2, xold);
         if (extrap) CK(cudaMemcpyAsync(xold, x0, g.n * 8, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));   // the previous solution
         std::swap(b, bprev);
