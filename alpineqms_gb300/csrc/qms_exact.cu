@@ -418,11 +418,23 @@ __global__ void qk_build_rhs(QGrid g, const uint8_t* __restrict__ ids, const QMa
     if (x_dirichlet && fixed) x_dirichlet[r] = val;
 }
 
+// a / c for a constant c with yc = RN(1/c): the quotient rounded once more through the exact
+// remainder (Markstein's FMA correction, IBM J. Res. Dev. 34(1), 1990): q = RN(a yc),
+// r = a - q c (exact with an FMA), result RN(q + r yc), which is the correctly rounded a / c
+// (checked bit for bit against the oracle's division in the tests)
+__device__ __forceinline__ double qms_div_const(double a, double c, double yc) {
+    const double q = a * yc;
+    const double r = fma(-q, c, a);
+    return fma(r, yc, q);
+}
+
 // The same right-hand side with the stored edge sigma, one thread per node (its up to four rows):
 // the same expressions as qk_build_rhs's stored-sigma path, without per-row index divisions.
+// idtd: 1 / (dt dx), 1 / (dt dy), 1 / (dt dz), each correctly rounded.
 __global__ void qk_build_rhs_nodes(QGrid g, Excite e, double dt, int tr, const double* __restrict__ xp,
                                    double* __restrict__ b, double* __restrict__ x_dirichlet,
-                                   const double* __restrict__ sg, const double* __restrict__ sdt) {
+                                   const double* __restrict__ sg, const double* __restrict__ sdt, double idtdx,
+                                   double idtdy, double idtdz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.Nx || j > g.Ny) return;
@@ -457,9 +469,9 @@ __global__ void qk_build_rhs_nodes(QGrid g, Excite e, double dt, int tr, const d
             const long long ax = qAX(g, i, j, k), axm = qAX(g, i - 1, j, k);
             const long long ay = qAY(g, i, j, k), aym = qAY(g, i, j - 1, k);
             const long long az = qAZ(g, i, j, k), azm = qAZ(g, i, j, k - 1);
-            val = (sg[ax] * xp[ax] - sg[axm] * xp[axm]) / (dt * dx)
-                + (sg[ay] * xp[ay] - sg[aym] * xp[aym]) / (dt * dy)
-                + (sg[az] * xp[az] - sg[azm] * xp[azm]) / (dt * dz);
+            val = qms_div_const(sg[ax] * xp[ax] - sg[axm] * xp[axm], dt * dx, idtdx)
+                + qms_div_const(sg[ay] * xp[ay] - sg[aym] * xp[aym], dt * dy, idtdy)
+                + qms_div_const(sg[az] * xp[az] - sg[azm] * xp[azm], dt * dz, idtdz);
         } else {
             val = 0.0;
         }
@@ -578,8 +590,9 @@ void qms_launch_rhs(const QGrid& g, const uint8_t* ids, const QMatTable<double>*
                     int tr, const double* xp, double* b, double* x_dirichlet, cudaStream_t st, const double* sg,
                     const double* sdt) {
     if (sg) {
-        qk_build_rhs_nodes<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, to_excite(ex), dt, tr, xp, b, x_dirichlet,
-                                                                           sg, sdt);
+        qk_build_rhs_nodes<<<qms_node_grid(g), qms_node_block(), 0, st>>>(
+            g, to_excite(ex), dt, tr, xp, b, x_dirichlet, sg, sdt, 1.0 / (dt * g.dx), 1.0 / (dt * g.dy),
+            1.0 / (dt * g.dz));
         return;
     }
     int bs = 256;

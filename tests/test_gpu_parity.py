@@ -355,15 +355,15 @@ def test_double_float_residual_agrees_with_fp64():
 
 
 @pytest.mark.gpu
-def test_transient_rhs_bit_exact():
+@pytest.mark.parametrize("xs,ys,zs,dt,seed", [(10, 9, 11, 1e-5, 5), (26, 24, 22, 2.7e-5, 11)])
+def test_transient_rhs_bit_exact(xs, ys, zs, dt, seed):
     """The solver's transient right-hand side (K7 with the per-geometry edge sigma and sigma / dt
-    stored once) equals the oracle's assembled RHS bit for bit."""
-    xs, ys, zs = 10, 9, 11
-    geom, props, d = make_case(xs, ys, zs, seed=5)
-    dt = 1e-5
+    stored once, the divisions by dt h through a corrected reciprocal) equals the oracle's
+    assembled RHS bit for bit."""
+    geom, props, d = make_case(xs, ys, zs, seed=seed)
     c = o.materials(xs, ys, zs, geom, props)
     n = o.sizes(xs, ys, zs)[0]
-    x = np.random.default_rng(7).standard_normal(n) * 1e-3
+    x = np.random.default_rng(7 + seed).standard_normal(n) * 1e-3
     v, B = (1.5, -0.5, 0.25), (2e-3, -1e-3, 5e-3)
     G = np.array([0.05, 0.02, -0.01, 0.02, -0.03, 0.04, -0.01, 0.04, -0.02])
     s = solver_for(xs, ys, zs, d, dt, geom, props)
