@@ -43,8 +43,8 @@ def parse_args():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=12,
-                    help="untimed steps; the first ~10 steps of a run adapt the FGMRES replay length and
-                         build up the extrapolated start (3 solutions)")
+                    help="untimed steps; the first ~10 steps of a run adapt the FGMRES replay length and "
+                         "build up the extrapolated start (3 solutions)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--size", type=int, default=256)
