@@ -202,6 +202,7 @@ int qms_set_state(qms_handle* h, const double* x_in) {
     CKH(cudaMemcpyAsync(h->s.x, x_in, h->s.g.n * 8, cudaMemcpyHostToDevice, h->s.st));
     CKH(cudaStreamSynchronize(h->s.st));
     h->s.rfin_ok = false;          // a new state: the next solve needs an exact anchor
+    h->s.hist_len = 0;             // ... and has no history to extrapolate
     return 0;
 }
 

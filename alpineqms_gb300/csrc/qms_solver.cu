@@ -477,7 +477,7 @@ void QmsSolver::release() {
     gm_H = gm_scal = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
                     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
-                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2};
+                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2, hist_x};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -490,6 +490,7 @@ void QmsSolver::release() {
     xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
     rsg = rsdt = nullptr;
     bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0; xold = xold2 = nullptr;
+    hist_x = nullptr; hist_len = 0;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -574,6 +575,7 @@ int QmsSolver::init(const qms_desc& d) {
         CK(cudaMalloc(&rsdt, g.oV * 8));
         CK(cudaMalloc(&bprev, n * 8));
         CK(cudaMalloc(&xold, n * 8));
+        CK(cudaMalloc(&hist_x, n * 8));
         if (d.extrapolate >= 2) CK(cudaMalloc(&xold2, n * 8));
         CK(pl_alloc((void**)&rfin, 8));
         CK(pl_alloc((void**)&dinvdf, 8));
@@ -614,7 +616,7 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     // the block-triangular preconditioner's V right-hand side; the double-float residual's x, b,
     // coefficients and FP32 result (mixed precision)
     size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
-    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4 + 8 + 8) + 6 * qms_pl(g).comp * 8 + 2 * g.n * 8 + 2 * g.oV * 8;
+    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4 + 8 + 8) + 6 * qms_pl(g).comp * 8 + 5 * g.n * 8 + 2 * g.oV * 8;
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
@@ -654,6 +656,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     if (rsg) qms_launch_rhs_coef(g, ids, dtab64, desc.dt, rsg, rsdt, st);
     if (dinvdf) qms_launch_dinv_df(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, true), dinvdf, st);
     rfin_ok = false;
+    hist_len = 0;
     QCoef<float> c32 = coef32();
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
@@ -1119,14 +1122,15 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // the previous solve's final residual anchors this one when the operator is the same
     const bool chain = df_resid && transient && rfin_ok && chain_len < 16 && chain_v[0] == v[0] &&
                        chain_v[1] == v[1] && chain_v[2] == v[2];
-    // a chained solve after a chained solve: x0 still holds the solution before the previous one
-    const bool extrap = chain && chain_len >= 1 && desc.extrapolate;
-    const bool quad = extrap && chain_len >= 2 && xold2;
+    // the start of a transient solve that follows solves with the same operator: an extrapolation
+    // of the last solutions (x = hist[0], the one before in hist[1], ...), independent of how the
+    // residual is anchored
+    const bool same_op = transient && chain_v[0] == v[0] && chain_v[1] == v[1] && chain_v[2] == v[2];
+    if (!same_op) hist_len = 0;
+    const bool extrap = same_op && desc.extrapolate > 0 && hist_len >= 2 && xold;
+    const bool quad = extrap && desc.extrapolate >= 2 && hist_len >= 3 && xold2;
     if (chain) {
-        // x0 is copied, not swapped: the captured refinement graphs hold its address (xold and
-        // xold2 are read by the extrapolation only)
-        if (xold2) std::swap(xold2, xold);
-        if (extrap) CK(cudaMemcpyAsync(xold, x0, g.n * 8, cudaMemcpyDeviceToDevice, st));
+        // x0 is copied, not swapped: the captured refinement graphs hold its address
         CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));   // the previous solution
         std::swap(b, bprev);
     }
@@ -1145,15 +1149,15 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         for (int q = 0; q < 3; q++) same = same && chain_B[q] == B[q];
         for (int q = 0; q < 9; q++) same = same && chain_G[q] == G[q];
         anchor_is_residual = same;
-        if (extrap) {
-            // start from the linear extrapolation of the last two states (Dirichlet rows keep the
-            // values just written); the first residual then follows incrementally from the anchor
-            qms_launch_extrapolate(g, x, xold, quad ? xold2 : nullptr, st);
-            nlaunch++;
-            anchor_is_residual = false;
-        }
     } else {
         chain_len = 0;
+    }
+    if (extrap) {
+        // the extrapolated start (Dirichlet rows keep the values just written); its residual then
+        // follows incrementally from the anchor, or is the FP64 anchor itself
+        qms_launch_extrapolate(g, x, xold, quad ? xold2 : nullptr, st);
+        nlaunch++;
+        anchor_is_residual = false;
     }
     rfin_ok = false;
     CK(cudaMemsetAsync(status, 0, 4, st));
@@ -1272,6 +1276,18 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // the final residual (rfin) anchors the next transient solve when it belongs to the state
     // that this solve leaves in x
     rfin_ok = df_resid && transient && last_resid_df && rel <= desc.tol;
+    // history of converged transient solutions for the extrapolated start (x itself is the newest;
+    // xold and xold2 the two before, rotated by pointer: only the extrapolation reads them)
+    if (transient && rel <= desc.tol && xold) {
+        double* freed = xold2 ? xold2 : xold;
+        if (xold2) xold2 = xold;
+        xold = hist_x;
+        hist_x = freed;
+        CK(cudaMemcpyAsync(hist_x, x, g.n * 8, cudaMemcpyDeviceToDevice, st));
+        hist_len = std::min(hist_len + 1, xold2 ? 3 : 2);
+    } else {
+        hist_len = 0;
+    }
     for (int q = 0; q < 3; q++) { chain_v[q] = v[q]; chain_B[q] = B[q]; }
     for (int q = 0; q < 9; q++) chain_G[q] = G[q];
     if (!(rel <= desc.tol) && best_rel < rel && std::isfinite(best_rel)) {

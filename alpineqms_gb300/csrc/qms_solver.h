@@ -67,8 +67,10 @@ struct QmsSolver {
     double chain_v[3] = {0, 0, 0};
     double chain_B[3] = {0, 0, 0}, chain_G[9] = {};
     bool anchor_is_residual = false;  // x is still the anchor state (same Dirichlet values)
-    double* xold = nullptr;     // the final state of the solve before the previous one (chained)
-    double* xold2 = nullptr;    // ... and of the one before that (quadratic extrapolation)
+    double* hist_x = nullptr;   // the last converged transient solution
+    double* xold = nullptr;     // the one before it
+    double* xold2 = nullptr;    // ... and the one before that (quadratic extrapolation)
+    int hist_len = 0;           // consecutive converged transient solves with the same operator (<= 3)
     double* rsg = nullptr;      // edge sigma of every A row, and / dt (transient right-hand side)
     double* rsdt = nullptr;
     qdf* xdf = nullptr;         // x - x0
