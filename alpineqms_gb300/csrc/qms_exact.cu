@@ -505,6 +505,24 @@ __global__ void qk_rhs_coef(QGrid g, const uint8_t* __restrict__ ids, const QMat
 }
 
 // K8: H at cell centres from the A blocks of x (F:1346-1376); cubes are xs*ys*zs, F-order.
+// H at cell (i, j, k) from the A blocks of x (F:1346-1376)
+__device__ __forceinline__ void qms_hcell(const QGrid& g, const ExactCoef& c, const double* __restrict__ x, int i, int j,
+                                          int k, double& hx, double& hy, double& hz) {
+    const double dx = g.dx, dy = g.dy, dz = g.dz;
+#define XAX(a, b_, d) x[qAX(g, a, b_, d)]
+#define XAY(a, b_, d) x[qAY(g, a, b_, d)]
+#define XAZ(a, b_, d) x[qAZ(g, a, b_, d)]
+    hx = 0.5 * (((XAZ(i, j + 1, k) - XAZ(i, j, k)) / dy - (XAY(i, j, k + 1) - XAY(i, j, k)) / dz) / c.mux(i, j, k) +
+                ((XAZ(i + 1, j + 1, k) - XAZ(i + 1, j, k)) / dy - (XAY(i + 1, j, k + 1) - XAY(i + 1, j, k)) / dz) / c.mux(i + 1, j, k));
+    hy = 0.5 * (((XAX(i, j, k + 1) - XAX(i, j, k)) / dz - (XAZ(i + 1, j, k) - XAZ(i, j, k)) / dx) / c.muy(i, j, k) +
+                ((XAX(i, j + 1, k + 1) - XAX(i, j + 1, k)) / dz - (XAZ(i + 1, j + 1, k) - XAZ(i, j + 1, k)) / dx) / c.muy(i, j + 1, k));
+    hz = 0.5 * (((XAY(i + 1, j, k) - XAY(i, j, k)) / dx - (XAX(i, j + 1, k) - XAX(i, j, k)) / dy) / c.muz(i, j, k) +
+                ((XAY(i + 1, j, k + 1) - XAY(i, j, k + 1)) / dx - (XAX(i, j + 1, k + 1) - XAX(i, j, k + 1)) / dy) / c.muz(i, j, k + 1));
+#undef XAX
+#undef XAY
+#undef XAZ
+}
+
 __global__ void qk_hfield(QGrid g, const uint8_t* __restrict__ ids, const QMatTable<double>* __restrict__ tab,
                           const double* __restrict__ x, double* __restrict__ Hx, double* __restrict__ Hy,
                           double* __restrict__ Hz) {
@@ -513,24 +531,26 @@ __global__ void qk_hfield(QGrid g, const uint8_t* __restrict__ ids, const QMatTa
     const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
     if (i > g.xs || j > g.ys || k > g.zs) return;
     ExactCoef c{g, ids, tab};
-    const double dx = g.dx, dy = g.dy, dz = g.dz;
-#define XAX(a, b_, d) x[qAX(g, a, b_, d)]
-#define XAY(a, b_, d) x[qAY(g, a, b_, d)]
-#define XAZ(a, b_, d) x[qAZ(g, a, b_, d)]
     const long long cq = qCELL(g, i, j, k);
-    Hx[cq] = 0.5 * (((XAZ(i, j + 1, k) - XAZ(i, j, k)) / dy - (XAY(i, j, k + 1) - XAY(i, j, k)) / dz) / c.mux(i, j, k) +
-                    ((XAZ(i + 1, j + 1, k) - XAZ(i + 1, j, k)) / dy - (XAY(i + 1, j, k + 1) - XAY(i + 1, j, k)) / dz) / c.mux(i + 1, j, k));
-    Hy[cq] = 0.5 * (((XAX(i, j, k + 1) - XAX(i, j, k)) / dz - (XAZ(i + 1, j, k) - XAZ(i, j, k)) / dx) / c.muy(i, j, k) +
-                    ((XAX(i, j + 1, k + 1) - XAX(i, j + 1, k)) / dz - (XAZ(i + 1, j + 1, k) - XAZ(i, j + 1, k)) / dx) / c.muy(i, j + 1, k));
-    Hz[cq] = 0.5 * (((XAY(i + 1, j, k) - XAY(i, j, k)) / dx - (XAX(i, j + 1, k) - XAX(i, j, k)) / dy) / c.muz(i, j, k) +
-                    ((XAY(i + 1, j, k + 1) - XAY(i, j, k + 1)) / dx - (XAX(i, j + 1, k + 1) - XAX(i, j, k + 1)) / dy) / c.muz(i, j, k + 1));
-#undef XAX
-#undef XAY
-#undef XAZ
+    qms_hcell(g, c, x, i, j, k, Hx[cq], Hy[cq], Hz[cq]);
 }
 
-// K8: the 2-D slice (axis 0/1/2 = x/y/z, 1-based index) of the three cubes into
-// out[3][n1*n2] in the record order of F:1380-1394.
+// H on the cells of one slice only (the same values as qk_hfield + qk_slice), in qk_slice's layout
+__global__ void qk_hslice(QGrid g, const uint8_t* __restrict__ ids, const QMatTable<double>* __restrict__ tab,
+                          const double* __restrict__ x, int axis, int index, double* __restrict__ out) {
+    int n1 = axis == 0 ? g.ys : g.xs;
+    int n2 = axis == 2 ? g.ys : g.zs;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n1 * n2) return;
+    int a = (int)(t % n1) + 1, b = (int)(t / n1) + 1;
+    int i, j, k;
+    if (axis == 0) { i = index; j = a; k = b; }
+    else if (axis == 1) { i = a; j = index; k = b; }
+    else { i = a; j = b; k = index; }
+    ExactCoef c{g, ids, tab};
+    const long long m = (long long)n1 * n2;
+    qms_hcell(g, c, x, i, j, k, out[t], out[m + t], out[2 * m + t]);
+}
 __global__ void qk_slice(QGrid g, int axis, int index, const double* __restrict__ Hx, const double* __restrict__ Hy,
                          const double* __restrict__ Hz, double* __restrict__ out) {
     int n1 = axis == 0 ? g.ys : g.xs;
@@ -612,6 +632,12 @@ void qms_launch_hfield(const QGrid& g, const uint8_t* ids, const QMatTable<doubl
     dim3 bs(32, 4, 2);
     dim3 gs((g.xs + 31) / 32, (g.ys + 3) / 4, (g.zs + 1) / 2);
     qk_hfield<<<gs, bs, 0, st>>>(g, ids, tab, x, Hx, Hy, Hz);
+}
+
+void qms_launch_hslice(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const double* x, int axis,
+                       int index, double* out, cudaStream_t st) {
+    long long m = (long long)(axis == 0 ? g.ys : g.xs) * (axis == 2 ? g.ys : g.zs);
+    qk_hslice<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(g, ids, tab, x, axis, index, out);
 }
 
 void qms_launch_slice(const QGrid& g, int axis, int index, const double* Hx, const double* Hy, const double* Hz,

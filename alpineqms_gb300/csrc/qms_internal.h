@@ -20,6 +20,9 @@ void qms_launch_rhs_coef(const QGrid& g, const uint8_t* ids, const QMatTable<dou
                          double* sdt, cudaStream_t st);
 void qms_launch_hfield(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const double* x, double* Hx,
                        double* Hy, double* Hz, cudaStream_t st);
+// H on the cells of one slice straight from x (qk_slice's layout)
+void qms_launch_hslice(const QGrid& g, const uint8_t* ids, const QMatTable<double>* tab, const double* x, int axis,
+                       int index, double* out, cudaStream_t st);
 void qms_launch_slice(const QGrid& g, int axis, int index, const double* Hx, const double* Hy, const double* Hz,
                       double* out, cudaStream_t st);
 void qms_launch_ids(long long ncell, const double* geom, const uint8_t* lut, int maxid, uint8_t* ids, unsigned* status,

@@ -1335,14 +1335,15 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
 int QmsSolver::fields(int which, int axis, int index, double* host_out) {
     CK(cudaSetDevice(dev));
     const long long ncell = (long long)g.xs * g.ys * g.zs;
-    qms_launch_hfield(g, ids, dtab64, x, H, H + ncell, H + 2 * ncell, st);
-    nlaunch++;
     if (which == QMS_FIELD_CUBES) {
+        qms_launch_hfield(g, ids, dtab64, x, H, H + ncell, H + 2 * ncell, st);
+        nlaunch++;
         CK(cudaMemcpyAsync(host_out, H, 3 * ncell * 8, cudaMemcpyDeviceToHost, st));
     } else {
         int lim = axis == 0 ? g.xs : axis == 1 ? g.ys : g.zs;
         if (axis < 0 || axis > 2 || index < 1 || index > lim) { err = "slice axis/index out of range"; return QMS_ERR_ARG; }
-        qms_launch_slice(g, axis, index, H, H + ncell, H + 2 * ncell, slicebuf, st);
+        // only the slice's cells (what the reference dumps every step)
+        qms_launch_hslice(g, ids, dtab64, x, axis, index, slicebuf, st);
         nlaunch++;
         long long m = (long long)(axis == 0 ? g.ys : g.xs) * (axis == 2 ? g.ys : g.zs);
         CK(cudaMemcpyAsync(host_out, slicebuf, 3 * m * 8, cudaMemcpyDeviceToHost, st));

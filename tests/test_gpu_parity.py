@@ -147,9 +147,12 @@ def test_rhs_and_hfield_bit_exact():
     Hr = o.hfield(xs, ys, zs, *d, c, x)
     for q in range(3):
         assert np.array_equal(H[q].ravel(order="F"), Hr[q])
-    sl = s.slices("y", 4)
-    for q in range(3):
-        assert np.array_equal(sl[q], H[q][:, 3, :])
+    for ax, idx in (("x", 1), ("x", xs), ("y", 4), ("y", ys), ("z", 1), ("z", 7)):
+        sl = s.slices(ax, idx)
+        cut = [slice(None)] * 3
+        cut["xyz".index(ax)] = idx - 1
+        for q in range(3):
+            assert np.array_equal(sl[q], H[q][tuple(cut)]), (ax, idx, q)
     s.close()
 
 
