@@ -70,6 +70,7 @@ int qms_create(const qms_desc* d, qms_handle** out) {
     if (!(dd.mg_alpha > 0)) dd.mg_alpha = 1.0;
     if (dd.mg_coarse_sweeps < 0) dd.mg_coarse_sweeps = 0;
     if (dd.mg_v_sweeps < 0) dd.mg_v_sweeps = 0;
+    dd.extrapolate = std::max(0, std::min(dd.extrapolate, 3));
     if (dd.max_inner <= 0 || dd.max_outer < 0 || !(dd.tol > 0) || !(dd.inner_rtol > 0) || dd.mg_sweeps < 1 ||
         !(dd.mg_omega > 0)) {
         std::lock_guard<std::mutex> lk(g_err_mu);
@@ -203,6 +204,8 @@ int qms_set_state(qms_handle* h, const double* x_in) {
     CKH(cudaStreamSynchronize(h->s.st));
     h->s.rfin_ok = false;          // a new state: the next solve needs an exact anchor
     h->s.hist_len = 0;             // ... and has no history to extrapolate
+    h->s.w_len = 0;
+    h->s.last_chained = false;
     return 0;
 }
 

@@ -89,6 +89,18 @@ __device__ double lift_v(const Excite& e, double xq, double yq, double zq) {
            - 0.5 * (vx * gy - vy * gx) * zq;
 }
 
+// One Dirichlet value (comp 0..2: A x, y, z; 3: V) at node (i, j, k), out of line: only boundary
+// threads of the node kernel call it, and inlined, its FP64 arithmetic would be if-converted
+// into every thread (FP64 issue is scarce on GB300)
+__device__ __noinline__ double lift_comp(const Excite& e, int comp, int i, int j, int k, double dx, double dy,
+                                         double dz) {
+    const double xq = (i - 1) * dx, yq = (j - 1) * dy, zq = (k - 1) * dz;
+    if (comp == 0) return lift_ax(e, xq, yq, zq);
+    if (comp == 1) return lift_ay(e, xq, yq, zq);
+    if (comp == 2) return lift_az(e, xq, yq, zq);
+    return lift_v(e, xq, yq, zq);
+}
+
 // number of interior rows before (i,j,k) in a block whose interior is the box
 // [ilo,ihi]x[jlo,jhi]x[klo,khi] (F-order traversal, i fastest)
 __device__ long long interior_before(int i, int j, int k, int ilo, int ihi, int jlo, int jhi, int klo, int khi) {
@@ -422,60 +434,61 @@ __global__ void qk_build_rhs(QGrid g, const uint8_t* __restrict__ ids, const QMa
 // remainder (Markstein's FMA correction, IBM J. Res. Dev. 34(1), 1990): q = RN(a yc),
 // r = a - q c (exact with an FMA), result RN(q + r yc), which is the correctly rounded a / c
 // (checked bit for bit against the oracle's division in the tests)
-__device__ __forceinline__ double qms_div_const(double a, double c, double yc) {
-    const double q = a * yc;
-    const double r = fma(-q, c, a);
-    return fma(r, yc, q);
+struct QDivC {
+    double c, yc;          // the divisor and RN(1 / c), both formed on the host
+};
+__device__ __forceinline__ double qms_div_const(double a, QDivC d) {
+    const double q = a * d.yc;
+    const double r = fma(-q, d.c, a);
+    return fma(r, d.yc, q);
 }
 
 // The same right-hand side with the stored edge sigma, one thread per node (its up to four rows):
 // the same expressions as qk_build_rhs's stored-sigma path, without per-row index divisions.
-// idtd: 1 / (dt dx), 1 / (dt dy), 1 / (dt dz), each correctly rounded.
+// dv*: dt dx, dt dy, dt dz and their correctly rounded reciprocals.  xp and x_dirichlet may be
+// the same vector: the Dirichlet rows written here are never read through xp (a V row that is
+// not a Dirichlet row reads the A rows of its own and the lower neighbour nodes, none of which
+// is a Dirichlet row).
 __global__ void qk_build_rhs_nodes(QGrid g, Excite e, double dt, int tr, const double* __restrict__ xp,
                                    double* __restrict__ b, double* __restrict__ x_dirichlet,
-                                   const double* __restrict__ sg, const double* __restrict__ sdt, double idtdx,
-                                   double idtdy, double idtdz) {
+                                   const double* __restrict__ sg, const double* __restrict__ sdt, QDivC dvx,
+                                   QDivC dvy, QDivC dvz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.Nx || j > g.Ny) return;
-    const double dx = g.dx, dy = g.dy, dz = g.dz;
-    const double xq = (i - 1) * dx, yq = (j - 1) * dy, zq = (k - 1) * dz;
-    auto put = [&](long long r, bool fixed, double val) {
+    // FP64 issue bounds this kernel (GB300's FP64 rate is a small fraction of its FP32 one): the
+    // the Dirichlet values (boundary rows) out of line, dt h from the host
+    auto row = [&](long long r, int comp, bool fixed) {
+        double val;
+        if (fixed) {
+            val = lift_comp(e, comp, i, j, k, g.dx, g.dy, g.dz);
+            if (x_dirichlet) x_dirichlet[r] = val;
+        } else {
+            val = tr ? sdt[r] * xp[r] : 0.0;
+        }
         b[r] = val;
-        if (x_dirichlet && fixed) x_dirichlet[r] = val;
     };
-    if (i <= g.xs) {
-        const long long r = qAX(g, i, j, k);
-        const bool fixed = qFixX(g, i, j, k);
-        put(r, fixed, fixed ? lift_ax(e, xq, yq, zq) : (tr ? sdt[r] * xp[r] : 0.0));
-    }
-    if (j <= g.ys) {
-        const long long r = qAY(g, i, j, k);
-        const bool fixed = qFixY(g, i, j, k);
-        put(r, fixed, fixed ? lift_ay(e, xq, yq, zq) : (tr ? sdt[r] * xp[r] : 0.0));
-    }
-    if (k <= g.zs) {
-        const long long r = qAZ(g, i, j, k);
-        const bool fixed = qFixZ(g, i, j, k);
-        put(r, fixed, fixed ? lift_az(e, xq, yq, zq) : (tr ? sdt[r] * xp[r] : 0.0));
-    }
+    if (i <= g.xs) row(qAX(g, i, j, k), 0, qFixX(g, i, j, k));
+    if (j <= g.ys) row(qAY(g, i, j, k), 1, qFixY(g, i, j, k));
+    if (k <= g.zs) row(qAZ(g, i, j, k), 2, qFixZ(g, i, j, k));
     {
         const long long r = qV(g, i, j, k);
         const bool fixed = qFixV(g, i, j, k);
         double val;
         if (fixed) {
-            val = lift_v(e, xq, yq, zq);
+            val = lift_comp(e, 3, i, j, k, g.dx, g.dy, g.dz);
         } else if (tr) {
             const long long ax = qAX(g, i, j, k), axm = qAX(g, i - 1, j, k);
             const long long ay = qAY(g, i, j, k), aym = qAY(g, i, j - 1, k);
             const long long az = qAZ(g, i, j, k), azm = qAZ(g, i, j, k - 1);
-            val = qms_div_const(sg[ax] * xp[ax] - sg[axm] * xp[axm], dt * dx, idtdx)
-                + qms_div_const(sg[ay] * xp[ay] - sg[aym] * xp[aym], dt * dy, idtdy)
-                + qms_div_const(sg[az] * xp[az] - sg[azm] * xp[azm], dt * dz, idtdz);
+            val = qms_div_const(sg[ax] * xp[ax] - sg[axm] * xp[axm], dvx)
+                + qms_div_const(sg[ay] * xp[ay] - sg[aym] * xp[aym], dvy)
+                + qms_div_const(sg[az] * xp[az] - sg[azm] * xp[azm], dvz);
         } else {
             val = 0.0;
         }
-        put(r, fixed, val);
+        b[r] = val;
+        if (x_dirichlet && fixed) x_dirichlet[r] = val;
     }
 }
 
@@ -611,8 +624,8 @@ void qms_launch_rhs(const QGrid& g, const uint8_t* ids, const QMatTable<double>*
                     const double* sdt) {
     if (sg) {
         qk_build_rhs_nodes<<<qms_node_grid(g), qms_node_block(), 0, st>>>(
-            g, to_excite(ex), dt, tr, xp, b, x_dirichlet, sg, sdt, 1.0 / (dt * g.dx), 1.0 / (dt * g.dy),
-            1.0 / (dt * g.dz));
+            g, to_excite(ex), dt, tr, xp, b, x_dirichlet, sg, sdt, QDivC{dt * g.dx, 1.0 / (dt * g.dx)},
+            QDivC{dt * g.dy, 1.0 / (dt * g.dy)}, QDivC{dt * g.dz, 1.0 / (dt * g.dz)});
         return;
     }
     int bs = 256;

@@ -254,16 +254,24 @@ __global__ void qk_dinv_df(QGrid g, QCoef<double> c, QStepPar<double> P, qdf* __
     out[3 * L.comp + t] = qdf_split(1.0 / d);
 }
 
-// The extrapolation of the state from the last steps on the rows that are not Dirichlet rows,
-// the start of the next solve: x = 2 x - xold (linear), or with xold2 (the step before)
-// x = 3 x - 3 xold + xold2 (quadratic)
+// The polynomial extrapolation of the state from the last solutions (x the newest, xo1 the one
+// before, ...), the start of the next solve: order 1 x = 2 x - xo1, order 2 x = 3 (x - xo1) + xo2,
+// order 3 x = 4 (x + xo2) - 6 xo1 - xo3
+__device__ __forceinline__ double qms_extrap(int order, double x, double x1, double x2, double x3) {
+    if (order == 1) return 2.0 * x - x1;
+    if (order == 2) return 3.0 * (x - x1) + x2;
+    return 4.0 * (x + x2) - 6.0 * x1 - x3;
+}
+
+// The extrapolated start on the rows that are not Dirichlet rows (those keep the values just
+// written)
 __global__ void qk_extrapolate(QGrid g, double* __restrict__ x, const double* __restrict__ xold,
-                               const double* __restrict__ xold2) {
+                               const double* __restrict__ xold2, const double* __restrict__ xold3, int order) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.Nx || j > g.Ny) return;
     auto one = [&](long long r) {
-        x[r] = xold2 ? 3.0 * (x[r] - xold[r]) + xold2[r] : 2.0 * x[r] - xold[r];
+        x[r] = qms_extrap(order, x[r], xold[r], order >= 2 ? xold2[r] : 0.0, order >= 3 ? xold3[r] : 0.0);
     };
     if (i <= g.xs && !qFixX(g, i, j, k)) one(qAX(g, i, j, k));
     if (j <= g.ys && !qFixY(g, i, j, k)) one(qAY(g, i, j, k));
@@ -287,6 +295,91 @@ __global__ void qk_chain_anchor(QGrid g, const qdf* __restrict__ rprev, const do
     if (j <= g.ys) one(qAY(g, i, j, k), L.comp + t);
     if (k <= g.zs) one(qAZ(g, i, j, k), 2 * L.comp + t);
     one(qV(g, i, j, k), 3 * L.comp + t);
+}
+
+// The start of a transient step chained to the previous one, in one pass over the unknowns:
+//   r0 = rfin + D^-1 (b - bprev)       the anchor (the residual of x_n, the previous solution,
+//                                      against the new b; the same expression as qk_chain_anchor)
+//   w  = r0_prev - rfin = D^-1 M (x_n - x_{n-1})    (into wnew; when the previous step's own
+//                                      anchor state was x_{n-1})
+// x extrapolated to order xo (qk_extrapolate's formulas), and with rfloat the residual of that
+// x by linearity from the anchor and the differences w of the last steps (w1 = the stored w of
+// the step before, w2 the one before that):
+//   xo 1: x = x_n + d_n                     r = r0 - w
+//   xo 2: x = x_n + 2 d_n - d_{n-1}         r = r0 - (2 w - w1)
+//   xo 3: x = x_n + 3 d_n - 3 d_{n-1} + d_{n-2}    r = r0 - (3 (w - w1) + w2)
+// (d_n = x_n - x_{n-1}; valid when the Dirichlet values are the same in all these states), into
+// rfloat (FP32), rfin (in full) and the partials |r_A|^2, |r_V|^2, |x_A|^2, |x_V|^2 of gridDim.x
+// (= the blocks of the launch, gridDim.x * 4).  One thread per unknown (blockIdx.y: the
+// component), no two pointers alias: every load of a thread is in flight at once, and the kernel
+// is a stream of ~14 vectors.  Node indices are 32-bit (a grid with 2^32 nodes would need
+// terabytes of solver state).
+__global__ void __launch_bounds__(256) qk_step_start(
+    QGrid g, qdf* __restrict__ rfin, const double* __restrict__ b, const double* __restrict__ bprev,
+    const qdf* __restrict__ dinv, qdf* __restrict__ r0, double* __restrict__ x, const double* __restrict__ xo1,
+    const double* __restrict__ xo2, const double* __restrict__ xo3, const int xo, qdf* __restrict__ wnew,
+    const qdf* __restrict__ w1, const qdf* __restrict__ w2, float* __restrict__ rfloat,
+    double* __restrict__ partials) {
+    const QPL L = qms_pl(g);
+    const int c = blockIdx.y;
+    const unsigned Nx = (unsigned)g.Nx, Nxy = (unsigned)g.Nx * (unsigned)g.Ny, Nn = (unsigned)g.Nn;
+    float racc = 0.f, xacc = 0.f;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < Nn; t += gridDim.x * blockDim.x) {
+        const unsigned kk = t / Nxy, rem = t - kk * Nxy, jj = rem / Nx;
+        const int i = (int)(rem - jj * Nx) + 1, j = (int)jj + 1, k = (int)kk + 1;
+        long long ref;
+        bool fix;
+        if (c == 0) {
+            if (i > g.xs) continue;
+            ref = qAX(g, i, j, k); fix = qFixX(g, i, j, k);
+        } else if (c == 1) {
+            if (j > g.ys) continue;
+            ref = qAY(g, i, j, k); fix = qFixY(g, i, j, k);
+        } else if (c == 2) {
+            if (k > g.zs) continue;
+            ref = qAZ(g, i, j, k); fix = qFixZ(g, i, j, k);
+        } else {
+            ref = qV(g, i, j, k); fix = qFixV(g, i, j, k);
+        }
+        const long long pl = c * L.comp + qms_pl_node(g, L, i, j, k);
+        const bool ex = xo > 0 && !fix;
+        const qdf rf = rfin[pl], di = dinv[pl];
+        const double bb = b[ref], bp = bprev[ref];
+        const qdf rp = wnew ? r0[pl] : qdf();
+        double xs = x[ref];
+        const double x1 = ex ? xo1[ref] : 0.0, x2 = ex && xo >= 2 ? xo2[ref] : 0.0, x3 = ex && xo >= 3 ? xo3[ref] : 0.0;
+        const qdf v1 = rfloat && xo >= 2 ? w1[pl] : qdf(), v2 = rfloat && xo >= 3 ? w2[pl] : qdf();
+        const qdf a = rf + qdf_split(bb - bp) * di;
+        r0[pl] = a;
+        const qdf w = rp - rf;
+        if (wnew) wnew[pl] = w;
+        if (ex) {
+            xs = qms_extrap(xo, xs, x1, x2, x3);
+            x[ref] = xs;
+        }
+        if (rfloat) {
+            qdf d = w;
+            if (xo == 2) d = (w + w) - v1;
+            else if (xo == 3) d = qdf(3.f) * (w - v1) + v2;
+            const qdf r = a - d;
+            rfloat[pl] = r.h;
+            rfin[pl] = r;
+            racc += r.h * r.h;
+            const float f = qdf_split(xs).h;
+            xacc += f * f;
+        }
+    }
+    if (!rfloat) return;
+    __shared__ double sh[32];
+    const long long nb = (long long)gridDim.x * gridDim.y, bid = blockIdx.x + (long long)gridDim.x * c;
+    const double sr = qBlockSum(racc, sh);
+    const double sx = qBlockSum(xacc, sh);
+    if (threadIdx.x == 0) {
+        partials[bid] = c < 3 ? sr : 0.0;
+        partials[nb + bid] = c < 3 ? 0.0 : sr;
+        partials[2 * nb + bid] = c < 3 ? sx : 0.0;
+        partials[3 * nb + bid] = c < 3 ? 0.0 : sx;
+    }
 }
 
 // The residual is the anchor itself (x is the anchor state): r = r0 into rfloat (FP32) and rfull,
@@ -553,8 +646,16 @@ void qms_launch_anchor_resid(const QGrid& g, const qdf* r0, const double* x, flo
     qk_anchor_resid<<<(unsigned)nb, 256, 0, st>>>(g, r0, x, rfloat, rfull, partials);
 }
 
-void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const double* xold2, cudaStream_t st) {
-    qk_extrapolate<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, x, xold, xold2);
+void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const double* xold2, const double* xold3,
+                            int order, cudaStream_t st) {
+    qk_extrapolate<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, x, xold, xold2, xold3, order);
+}
+
+void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
+                           const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st) {
+    // nb partials per quantity: nb / 4 blocks per component
+    qk_step_start<<<dim3((unsigned)(nb / 4), 4), 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3,
+                                                               h.xo, h.wnew, h.w1, h.w2, rfloat, partials);
 }
 
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st) {

@@ -28,8 +28,24 @@ void qms_launch_resid_df(const QGrid& g, const QStepPar<qdf>& P, const CUtensorM
 // the residual when x is the anchor state: rfloat = (float) r0, rfull = r0, the four partials of nb blocks
 void qms_launch_anchor_resid(const QGrid& g, const qdf* r0, const double* x, float* rfloat, qdf* rfull,
                              double* partials, long long nb, cudaStream_t st);
-// x = 2 x - xold, or with xold2 3 x - 3 xold + xold2, on the non-Dirichlet rows (reference order)
-void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const double* xold2, cudaStream_t st);
+// x = the extrapolation of order 1..3 from x, xold, xold2, xold3 on the non-Dirichlet rows
+// (reference order)
+void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const double* xold2, const double* xold3,
+                            int order, cudaStream_t st);
+// the state history that the chained step start reads (qk_step_start)
+struct QStepStart {
+    double* x;                      // x_n, extrapolated in place when xo > 0
+    const double* xo1;              // x_{n-1}, x_{n-2}, x_{n-3}
+    const double* xo2;
+    const double* xo3;
+    int xo;                         // extrapolation order (0: x unchanged)
+    qdf* wnew;                      // where w = D^-1 M (x_n - x_{n-1}) goes (null: not formed)
+    const qdf* w1;                  // the stored w of the step before, and the one before that
+    const qdf* w2;                  // (no two of x, xo*, wnew, w1, w2 alias)
+};
+// nb (a multiple of 4): the blocks of the launch and the partials per quantity
+void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
+                           const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st);
 // 1 / diag M as double-float (padded layout)
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st);
 // r0 = rprev + D^-1 (b - bprev)   (b, bprev in reference order; the rest padded, double-float)

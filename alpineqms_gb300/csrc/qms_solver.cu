@@ -477,7 +477,7 @@ void QmsSolver::release() {
     gm_H = gm_scal = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
                     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
-                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2, hist_x};
+                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2, hist_x, xold3, wh[0], wh[1], wh[2]};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     for (auto& p : vec) if (p) cudaFree(p);
@@ -490,7 +490,8 @@ void QmsSolver::release() {
     xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
     rsg = rsdt = nullptr;
     bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0; xold = xold2 = nullptr;
-    hist_x = nullptr; hist_len = 0;
+    hist_x = nullptr; hist_len = 0; xold3 = nullptr; wh[0] = wh[1] = wh[2] = nullptr; w_len = 0; last_chained = false;
+    field_run = 0; start_resid_ready = false;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
 }
@@ -577,6 +578,8 @@ int QmsSolver::init(const qms_desc& d) {
         CK(cudaMalloc(&xold, n * 8));
         CK(cudaMalloc(&hist_x, n * 8));
         if (d.extrapolate >= 2) CK(cudaMalloc(&xold2, n * 8));
+        if (d.extrapolate >= 3) CK(cudaMalloc(&xold3, n * 8));
+        for (int q = 0; q < std::min(d.extrapolate, 3); q++) CK(pl_alloc((void**)&wh[q], 8));
         CK(pl_alloc((void**)&rfin, 8));
         CK(pl_alloc((void**)&dinvdf, 8));
         CK(cudaMalloc(&x0, n * 8));
@@ -616,7 +619,8 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     // the block-triangular preconditioner's V right-hand side; the double-float residual's x, b,
     // coefficients and FP32 result (mixed precision)
     size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
-    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4 + 8 + 8) + 6 * qms_pl(g).comp * 8 + 5 * g.n * 8 + 2 * g.oV * 8;
+    if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4 + 8 + 8) + 6 * qms_pl(g).comp * 8 + 5 * g.n * 8 + 2 * g.oV * 8 +
+                        (d.extrapolate >= 3 ? g.n * 8 : 0) + std::max(0, std::min(d.extrapolate, 3)) * qms_pl(g).n * 8;
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
@@ -657,6 +661,8 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     if (dinvdf) qms_launch_dinv_df(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, true), dinvdf, st);
     rfin_ok = false;
     hist_len = 0;
+    w_len = 0;
+    last_chained = false;
     QCoef<float> c32 = coef32();
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, false), dg_steady, st);
     qms_launch_diag_pl(g, c32, qms_step_par<float>(g, 0, 0, 0, desc.dt, true), dg_tr, st);
@@ -984,7 +990,13 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
 }
 
 void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], bool exact) {
-    if (df_resid && anchor_ready && anchor_is_residual && !exact) {
+    if (start_resid_ready && !exact) {
+        // the step start (qk_step_start) formed this residual and its partials
+        start_resid_ready = false;
+        last_resid_df = true;
+        finalize(FIN_RESID, 4, start_nb());
+        return;
+    } else if (df_resid && anchor_ready && anchor_is_residual && !exact) {
         // x is the anchor state: the residual is the anchor's
         OpEv* ev = prof_begin(3, (double)g.n * 8 * 3);
         qms_launch_anchor_resid(g, r0df, x, rpl, rfin, part, nbop, st);
@@ -1005,8 +1017,9 @@ void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], boo
     } else {
         QStepPar<double> P = qms_step_par<double>(g, v[0], v[1], v[2], desc.dt, transient);
         op<double>(adv, QOPH_RESID, P, x, b, r64, nullptr, part);
-        if (df_resid) {
-            // the anchor of the double-float residuals that follow in this solve
+        if (df_resid && !exact) {
+            // the anchor of the double-float residuals that follow in this solve (an exact
+            // residual asked for between solves leaves the anchor and its chain as they are)
             qms_launch_split_ref_pl(g, r64, r0df, rpl, st);
             cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st);
             nlaunch++;
@@ -1127,8 +1140,18 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // residual is anchored
     const bool same_op = transient && chain_v[0] == v[0] && chain_v[1] == v[1] && chain_v[2] == v[2];
     if (!same_op) hist_len = 0;
-    const bool extrap = same_op && desc.extrapolate > 0 && hist_len >= 2 && xold;
-    const bool quad = extrap && desc.extrapolate >= 2 && hist_len >= 3 && xold2;
+    // order of the extrapolation: the known solutions (hist_len, x_n included) less one
+    const int xo = !same_op || !xold ? 0 : std::max(0, std::min(std::min(desc.extrapolate, 3), hist_len - 1));
+    bool same_field = true;
+    for (int q = 0; q < 3; q++) same_field = same_field && chain_B[q] == B[q];
+    for (int q = 0; q < 9; q++) same_field = same_field && chain_G[q] == G[q];
+    field_run = same_field ? field_run + 1 : 1;
+    // w_n = D^-1 M (x_n - x_{n-1}) follows when this solve and the last one are chained; the
+    // residual of the extrapolated start then follows from the w of the last xo steps when the
+    // Dirichlet values did not change over them
+    const bool wcalc = chain && last_chained && wh[0];
+    const bool start_fused = wcalc && xo > 0 && w_len >= xo - 1 && field_run >= xo + 2;
+    start_resid_ready = false;
     if (chain) {
         // x0 is copied, not swapped: the captured refinement graphs hold its address
         CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));   // the previous solution
@@ -1140,25 +1163,36 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     anchor_ready = false;          // the first residual of this solve is the FP64 anchor ...
     anchor_is_residual = false;
     if (chain) {                   // ... unless it follows from the previous one
-        qms_launch_chain_anchor(g, rfin, b, bprev, dinvdf, r0df, st);
+        // the anchor, w_n and the extrapolated start in one pass; the residual of that start too
+        // when start_fused (otherwise the double-float residual from the anchor follows)
+        const int nw = std::min(desc.extrapolate, 3);          // w buffers: w_(n-1), w_(n-2), the new one
+        QStepStart hs{x, xold, xold2, xold3, xo, wcalc ? wh[nw - 1] : nullptr, wh[0], wh[1]};
+        OpEv* ev = start_fused ? prof_begin(3, (double)g.n * (8 * 11 + 8 * 2 * xo + 4)) : nullptr;
+        qms_launch_step_start(g, rfin, b, bprev, dinvdf, r0df, hs, start_fused ? rpl : nullptr, part, start_nb(), st);
         nlaunch++;
+        prof_end(ev);
+        if (wcalc) {               // wh[0]: w_n, wh[1]: w_(n-1), the oldest becomes the next one's buffer
+            qdf* fresh = wh[nw - 1];
+            for (int q = nw - 1; q > 0; q--) wh[q] = wh[q - 1];
+            wh[0] = fresh;
+        }
+        w_len = wcalc ? std::min(w_len + 1, std::max(1, nw - 1)) : 0;
         anchor_ready = true;
         chain_len++;
-        // same field: the Dirichlet values did not move, x is the anchor state
-        bool same = true;
-        for (int q = 0; q < 3; q++) same = same && chain_B[q] == B[q];
-        for (int q = 0; q < 9; q++) same = same && chain_G[q] == G[q];
-        anchor_is_residual = same;
+        // same field and no extrapolation: the Dirichlet values did not move, x is the anchor state
+        anchor_is_residual = same_field && xo == 0;
+        start_resid_ready = start_fused;
     } else {
         chain_len = 0;
+        w_len = 0;
+        if (xo > 0) {
+            // the extrapolated start (Dirichlet rows keep the values just written); its residual
+            // is the FP64 anchor
+            qms_launch_extrapolate(g, x, xold, xold2, xold3, xo, st);
+            nlaunch++;
+        }
     }
-    if (extrap) {
-        // the extrapolated start (Dirichlet rows keep the values just written); its residual then
-        // follows incrementally from the anchor, or is the FP64 anchor itself
-        qms_launch_extrapolate(g, x, xold, quad ? xold2 : nullptr, st);
-        nlaunch++;
-        anchor_is_residual = false;
-    }
+    last_chained = chain;
     rfin_ok = false;
     CK(cudaMemsetAsync(status, 0, 4, st));
     const bool adv = v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
@@ -1279,14 +1313,16 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // history of converged transient solutions for the extrapolated start (x itself is the newest;
     // xold and xold2 the two before, rotated by pointer: only the extrapolation reads them)
     if (transient && rel <= desc.tol && xold) {
-        double* freed = xold2 ? xold2 : xold;
+        double* freed = xold3 ? xold3 : xold2 ? xold2 : xold;
+        if (xold3) xold3 = xold2;
         if (xold2) xold2 = xold;
         xold = hist_x;
         hist_x = freed;
         CK(cudaMemcpyAsync(hist_x, x, g.n * 8, cudaMemcpyDeviceToDevice, st));
-        hist_len = std::min(hist_len + 1, xold2 ? 3 : 2);
+        hist_len = std::min(hist_len + 1, xold3 ? 4 : xold2 ? 3 : 2);
     } else {
         hist_len = 0;
+        last_chained = false;
     }
     for (int q = 0; q < 3; q++) { chain_v[q] = v[q]; chain_B[q] = B[q]; }
     for (int q = 0; q < 9; q++) chain_G[q] = G[q];

@@ -70,7 +70,19 @@ struct QmsSolver {
     double* hist_x = nullptr;   // the last converged transient solution
     double* xold = nullptr;     // the one before it
     double* xold2 = nullptr;    // ... and the one before that (quadratic extrapolation)
-    int hist_len = 0;           // consecutive converged transient solves with the same operator (<= 3)
+    double* xold3 = nullptr;    // ... and the one before that (cubic)
+    int hist_len = 0;           // consecutive converged transient solves with the same operator (<= 4)
+    // Residual of the extrapolated start by linearity (qk_step_start): w_n = D^-1 M (x_n - x_{n-1})
+    // is the difference of a chained solve's anchor and final residual; wh[0] holds the last
+    // step's, wh[1] the one before (cubic), w_len of them valid; one more buffer takes the next
+    qdf* wh[3] = {nullptr, nullptr, nullptr};
+    int w_len = 0;
+    bool last_chained = false;  // the last solve's anchor state was the solution before it
+    int field_run = 0;          // consecutive solves (this one included) with the same B, G
+    bool start_resid_ready = false;   // the step start formed the first residual
+    // blocks of the step start's launch (and its partials per quantity): a multiple of 4 within
+    // the partial buffer's 4 nbop + 64
+    long long start_nb() const { return 4 * std::max(1LL, nbop / 4); }
     double* rsg = nullptr;      // edge sigma of every A row, and / dt (transient right-hand side)
     double* rsdt = nullptr;
     qdf* xdf = nullptr;         // x - x0

@@ -41,7 +41,7 @@ UNIT = "DOF-timesteps/s"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=12,
                     help="untimed steps; the first ~10 steps of a run adapt the FGMRES replay length and "
                          "build up the extrapolated start (3 solutions)")
@@ -277,6 +277,9 @@ def run_gpu(args):
     st0 = solver.steady(sched.steady(), B, G)
     steady_s = time.perf_counter() - t0
     counter = 0
+    # the refinement graphs replayed in the timed region carry the profile's event records: they
+    # are captured during the warm-up, with the profile on
+    solver.profile_enable(True)
     for _ in range(args.warmup):
         counter += 1
         solver.step(sched.step(counter), B, G)
@@ -288,7 +291,7 @@ def run_gpu(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    solver.profile_enable(True)
+    solver.profile_enable(True)          # counts from here
     clocks.start()
     ev0.record(ext)
     for _ in range(args.steps):
@@ -310,6 +313,10 @@ def run_gpu(args):
     if not args.no_e2e:
         hostbuf = torch.empty(15, dtype=torch.float64).pin_memory()
         slice_bytes = 3 * inp.slice_shape()[0] * inp.slice_shape()[1] * 8
+        # two untimed steps capture the graphs without the profile's event records
+        for _ in range(2):
+            counter += 1
+            solver.step(sched.step(counter), B, G)
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -417,7 +424,8 @@ def run_gpu(args):
                 "accuracy": accuracy,
                 "clocks": clk, "steady_s": steady_s,
                 "steady_iters": {"outer": st0["outer"], "inner": st0["inner"]},
-                "step_iters": [{"outer": s["outer"], "inner": s["inner"], "r": s["r"]} for s in iters]}
+                "step_iters": [{"outer": s["outer"], "inner": s["inner"], "r0": s["r0"], "r": s["r"]}
+                               for s in iters]}
         print(json.dumps(line))
     solver.close()
     if dist:

@@ -111,7 +111,8 @@ typedef struct {
     int extrapolate;         /* a transient step that follows steps with the same operator starts
                                 from an extrapolation of the last solutions instead of x_n:
                                 2 (default) quadratic once three are known, 3 x_n - 3 x_(n-1) +
-                                x_(n-2) (linear before); 1 linear, 2 x_n - x_(n-1); 0 none */
+                                x_(n-2) (linear before); 1 linear, 2 x_n - x_(n-1); 3 cubic once
+                                four are known, 4 x_n - 6 x_(n-1) + 4 x_(n-2) - x_(n-3); 0 none */
 } qms_desc;
 
 typedef struct {

@@ -358,6 +358,44 @@ def test_double_float_residual_agrees_with_fp64():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_extrapolated_start_residual_by_linearity(order):
+    """Once three steps in a row are chained, the residual of the extrapolated start follows from
+    the anchor and the stored differences D^-1 M (x_n - x_(n-1)) of the last steps, without a
+    stencil pass (qk_step_start).  At the last step it must equal the exact FP64 residual of the
+    same start state (rebuilt here from the returned solutions), and every step must still reach
+    the tolerance with a final residual that agrees with the exact one."""
+    p, geom = _conductor_case(True)
+    from alpineqms_gb300.trajectory import VelocitySchedule
+    from alpineqms_gb300.inputs import Trajectory
+    sched = VelocitySchedule([Trajectory(1, *t) for t in p["traj"]], p["dt"])
+    s = solver_for(p["xs"], p["ys"], p["zs"], (p["dx"], p["dy"], p["dz"]), p["dt"], geom, p["props"],
+                   precision="mixed", extrapolate=order)
+    B, G = np.asarray(p["B"], np.float64), np.asarray(p["G"], np.float64).ravel()
+    s.steady(sched.steady(), B, G)
+    v = sched.step(1)                    # one constant frame velocity: every step has the same operator
+    X = []
+    for n in range(1, 8):
+        st = s.step(v, B, G)
+        assert st["status"] == 0, (n, st)
+        exact = s.residual_norm(True, v)
+        assert abs(st["r"] - exact) <= 0.25 * exact + 5e-15, (n, st["r"], exact)
+        X.append(s.get_state())
+    # the start of the last step: the solutions before it, extrapolated
+    if order == 1:
+        x_start = 2.0 * X[-2] - X[-3]
+    elif order == 2:
+        x_start = 3.0 * (X[-2] - X[-3]) + X[-4]
+    else:
+        x_start = 4.0 * (X[-2] + X[-4]) - 6.0 * X[-3] - X[-5]
+    s.set_state(x_start)                 # b is still the last step's
+    exact0 = s.residual_norm(True, v)
+    s.close()
+    assert exact0 > 0
+    assert abs(st["r0"] - exact0) <= 1e-3 * exact0 + 1e-15, (st["r0"], exact0)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("xs,ys,zs,dt,seed", [(10, 9, 11, 1e-5, 5), (26, 24, 22, 2.7e-5, 11)])
 def test_transient_rhs_bit_exact(xs, ys, zs, dt, seed):
     """The solver's transient right-hand side (K7 with the per-geometry edge sigma and sigma / dt
