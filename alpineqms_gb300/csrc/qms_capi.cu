@@ -51,7 +51,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->mg_region_cut = 0.0;
     d->mg_alpha = 1.5;
     d->mg_coupling = 1;
-    d->extrapolate = 2;
+    d->extrapolate = 3;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }
@@ -191,6 +191,7 @@ int qms_get_rhs(qms_handle* h, double* b_out) {
     HCHECK(h);
     if (!b_out) return QMS_ERR_ARG;
     CKH(cudaSetDevice(h->s.dev));
+    h->s.ensure_b();
     CKH(cudaMemcpyAsync(b_out, h->s.b, h->s.g.n * 8, cudaMemcpyDeviceToHost, h->s.st));
     CKH(cudaStreamSynchronize(h->s.st));
     return 0;
@@ -264,6 +265,7 @@ int qms_residual_norm(qms_handle* h, int transient, const double v[3], double* r
     QmsSolver& s = h->s;
     CKH(cudaSetDevice(s.dev));
     const bool adv = v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
+    s.ensure_b();
     int rc = s.residual(adv, transient != 0, v, true);
     if (rc) return rc;
     double xn = std::sqrt(s.hS[0 + 2] + s.hS[0 + 3]);

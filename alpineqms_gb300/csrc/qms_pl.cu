@@ -256,11 +256,11 @@ __global__ void qk_dinv_df(QGrid g, QCoef<double> c, QStepPar<double> P, qdf* __
 
 // The polynomial extrapolation of the state from the last solutions (x the newest, xo1 the one
 // before, ...), the start of the next solve: order 1 x = 2 x - xo1, order 2 x = 3 (x - xo1) + xo2,
-// order 3 x = 4 (x + xo2) - 6 xo1 - xo3
+// order 3 x = 4 (x + xo2) - 6 xo1 - xo3; in fused multiply-adds (1, 2, 3 FP64 operations)
 __device__ __forceinline__ double qms_extrap(int order, double x, double x1, double x2, double x3) {
-    if (order == 1) return 2.0 * x - x1;
-    if (order == 2) return 3.0 * (x - x1) + x2;
-    return 4.0 * (x + x2) - 6.0 * x1 - x3;
+    if (order == 1) return fma(2.0, x, -x1);
+    if (order == 2) return fma(3.0, x - x1, x2);
+    return fma(-6.0, x1, fma(4.0, x + x2, -x3));
 }
 
 // The extrapolated start on the rows that are not Dirichlet rows (those keep the values just
@@ -298,8 +298,8 @@ __global__ void qk_chain_anchor(QGrid g, const qdf* __restrict__ rprev, const do
 }
 
 // The start of a transient step chained to the previous one, in one pass over the unknowns:
-//   r0 = rfin + D^-1 (b - bprev)       the anchor (the residual of x_n, the previous solution,
-//                                      against the new b; the same expression as qk_chain_anchor)
+//   r0 = rfin + D^-1 (b - b_prev)      the anchor: the residual of x_n, the previous solution,
+//                                      against the new right-hand side
 //   w  = r0_prev - rfin = D^-1 M (x_n - x_{n-1})    (into wnew; when the previous step's own
 //                                      anchor state was x_{n-1})
 // x extrapolated to order xo (qk_extrapolate's formulas), and with rfloat the residual of that
@@ -309,58 +309,101 @@ __global__ void qk_chain_anchor(QGrid g, const qdf* __restrict__ rprev, const do
 //   xo 2: x = x_n + 2 d_n - d_{n-1}         r = r0 - (2 w - w1)
 //   xo 3: x = x_n + 3 d_n - 3 d_{n-1} + d_{n-2}    r = r0 - (3 (w - w1) + w2)
 // (d_n = x_n - x_{n-1}; valid when the Dirichlet values are the same in all these states), into
-// rfloat (FP32), rfin (in full) and the partials |r_A|^2, |r_V|^2, |x_A|^2, |x_V|^2 of gridDim.x
-// (= the blocks of the launch, gridDim.x * 4).  One thread per unknown (blockIdx.y: the
-// component), no two pointers alias: every load of a thread is in flight at once, and the kernel
-// is a stream of ~14 vectors.  Node indices are 32-bit (a grid with 2^32 nodes would need
-// terabytes of solver state).
+// rfloat (FP32), rfin (in full) and the partials |r_A|^2, |r_V|^2, |x_A|^2, |x_V|^2 of the
+// launch's blocks.
+// b - b_prev comes either from the two FP64 right-hand sides (b, bprev), or, with hx (a copy of
+// x_n) and the edge sigma sg, sdt = sg / dt, from the linear map that forms the transient
+// right-hand side, applied to d_n = hx - xo1 in double-float (the Dirichlet values unchanged):
+//   A rows  sdt d_n,    V rows  sum over the axes (sg_e d_e - sg_e' d_e') / (dt h)
+// with e, e' the node's two incident edges along the axis.  That skips the FP64 right-hand side
+// (FP64 issue is scarce on GB300); x0 then receives x_n here.
+// A block is 64 nodes x 4 components (thread c = threadIdx.x / 64): the V rows take the
+// products sg_e d_e of their own node's edges and of the edge before along x from the A threads
+// through shared memory.  Node indices are 32-bit (2^32 nodes would need terabytes of state).
+struct QStartRhs {
+    const double* hx;               // x_n (null: b - b_prev from b and bprev)
+    const double* sg;
+    const double* sdt;
+    qdf idt[3];                     // 1 / (dt dx), 1 / (dt dy), 1 / (dt dz)
+    double* x0;                     // receives x_n
+};
 __global__ void __launch_bounds__(256) qk_step_start(
     QGrid g, qdf* __restrict__ rfin, const double* __restrict__ b, const double* __restrict__ bprev,
     const qdf* __restrict__ dinv, qdf* __restrict__ r0, double* __restrict__ x, const double* __restrict__ xo1,
     const double* __restrict__ xo2, const double* __restrict__ xo3, const int xo, qdf* __restrict__ wnew,
     const qdf* __restrict__ w1, const qdf* __restrict__ w2, float* __restrict__ rfloat,
-    double* __restrict__ partials) {
+    double* __restrict__ partials, const QStartRhs R) {
+    __shared__ qdf prod[3][64];
     const QPL L = qms_pl(g);
-    const int c = blockIdx.y;
+    const int c = threadIdx.x >> 6, lane = threadIdx.x & 63;
     const unsigned Nx = (unsigned)g.Nx, Nxy = (unsigned)g.Nx * (unsigned)g.Ny, Nn = (unsigned)g.Nn;
+    const double* __restrict__ hx = R.hx;
+    const double* __restrict__ sg = R.sg;
     float racc = 0.f, xacc = 0.f;
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < Nn; t += gridDim.x * blockDim.x) {
-        const unsigned kk = t / Nxy, rem = t - kk * Nxy, jj = rem / Nx;
+    for (unsigned base = blockIdx.x * 64u; base < Nn; base += gridDim.x * 64u) {
+        const unsigned t = base + lane;
+        const bool valid = t < Nn;
+        const unsigned tt = valid ? t : 0u;
+        const unsigned kk = tt / Nxy, rem = tt - kk * Nxy, jj = rem / Nx;
         const int i = (int)(rem - jj * Nx) + 1, j = (int)jj + 1, k = (int)kk + 1;
+        bool has;
         long long ref;
         bool fix;
-        if (c == 0) {
-            if (i > g.xs) continue;
-            ref = qAX(g, i, j, k); fix = qFixX(g, i, j, k);
-        } else if (c == 1) {
-            if (j > g.ys) continue;
-            ref = qAY(g, i, j, k); fix = qFixY(g, i, j, k);
-        } else if (c == 2) {
-            if (k > g.zs) continue;
-            ref = qAZ(g, i, j, k); fix = qFixZ(g, i, j, k);
-        } else {
-            ref = qV(g, i, j, k); fix = qFixV(g, i, j, k);
-        }
+        if (c == 0) { has = valid && i <= g.xs; ref = has ? qAX(g, i, j, k) : 0; fix = qFixX(g, i, j, k); }
+        else if (c == 1) { has = valid && j <= g.ys; ref = has ? qAY(g, i, j, k) : 0; fix = qFixY(g, i, j, k); }
+        else if (c == 2) { has = valid && k <= g.zs; ref = has ? qAZ(g, i, j, k) : 0; fix = qFixZ(g, i, j, k); }
+        else { has = valid; ref = has ? qV(g, i, j, k) : 0; fix = qFixV(g, i, j, k); }
         const long long pl = c * L.comp + qms_pl_node(g, L, i, j, k);
-        const bool ex = xo > 0 && !fix;
-        const qdf rf = rfin[pl], di = dinv[pl];
-        const double bb = b[ref], bp = bprev[ref];
-        const qdf rp = wnew ? r0[pl] : qdf();
-        double xs = x[ref];
-        const double x1 = ex ? xo1[ref] : 0.0, x2 = ex && xo >= 2 ? xo2[ref] : 0.0, x3 = ex && xo >= 3 ? xo3[ref] : 0.0;
-        const qdf v1 = rfloat && xo >= 2 ? w1[pl] : qdf(), v2 = rfloat && xo >= 3 ? w2[pl] : qdf();
-        const qdf a = rf + qdf_split(bb - bp) * di;
+        const bool ex = has && xo > 0 && !fix;
+        double xs = 0.0, x1 = 0.0;
+        qdf db;
+        if (has) {
+            xs = x[ref];
+            if (ex || (hx && !fix)) x1 = xo1[ref];
+        }
+        if (hx) {
+            // the right-hand side's change from d_n; the A threads leave sg_e d_e for the V rows
+            if (c < 3) {
+                qdf p, q;
+                if (has && !fix) {
+                    const qdf d = qdf_split(hx[ref] - x1);
+                    p = qdf_split(sg[ref]) * d;
+                    q = qdf_split(R.sdt[ref]) * d;
+                }
+                prod[c][lane] = p;
+                db = q;
+            }
+            __syncthreads();
+            if (c == 3 && has && !fix) {
+                // edge products of the V row's incident edges: its own node's from shared memory,
+                // the ones before along y and z (and along x at the first lane) formed here
+                auto edge = [&](long long e) { return qdf_split(sg[e]) * qdf_split(hx[e] - xo1[e]); };
+                const qdf pxm = lane > 0 ? prod[0][lane - 1] : edge(qAX(g, i - 1, j, k));
+                db = (prod[0][lane] - pxm) * R.idt[0] + (prod[1][lane] - edge(qAY(g, i, j - 1, k))) * R.idt[1] +
+                     (prod[2][lane] - edge(qAZ(g, i, j, k - 1))) * R.idt[2];
+            }
+            __syncthreads();
+        } else if (has) {
+            db = qdf_split(b[ref] - bprev[ref]);
+        }
+        if (!has) continue;
+        const qdf rf = rfin[pl];
+        const qdf a = rf + db * dinv[pl];
+        qdf w;
+        if (wnew) {
+            w = r0[pl] - rf;
+            wnew[pl] = w;
+        }
         r0[pl] = a;
-        const qdf w = rp - rf;
-        if (wnew) wnew[pl] = w;
+        if (R.x0) R.x0[ref] = xs;
         if (ex) {
-            xs = qms_extrap(xo, xs, x1, x2, x3);
+            xs = qms_extrap(xo, xs, x1, xo >= 2 ? xo2[ref] : 0.0, xo >= 3 ? xo3[ref] : 0.0);
             x[ref] = xs;
         }
         if (rfloat) {
             qdf d = w;
-            if (xo == 2) d = (w + w) - v1;
-            else if (xo == 3) d = qdf(3.f) * (w - v1) + v2;
+            if (xo == 2) d = (w + w) - w1[pl];
+            else if (xo == 3) d = qdf(3.f) * (w - w1[pl]) + w2[pl];
             const qdf r = a - d;
             rfloat[pl] = r.h;
             rfin[pl] = r;
@@ -371,15 +414,15 @@ __global__ void __launch_bounds__(256) qk_step_start(
     }
     if (!rfloat) return;
     __shared__ double sh[32];
-    const long long nb = (long long)gridDim.x * gridDim.y, bid = blockIdx.x + (long long)gridDim.x * c;
-    const double sr = qBlockSum(racc, sh);
-    const double sx = qBlockSum(xacc, sh);
-    if (threadIdx.x == 0) {
-        partials[bid] = c < 3 ? sr : 0.0;
-        partials[nb + bid] = c < 3 ? 0.0 : sr;
-        partials[2 * nb + bid] = c < 3 ? sx : 0.0;
-        partials[3 * nb + bid] = c < 3 ? 0.0 : sx;
-    }
+    const long long nb = gridDim.x;
+    double s = qBlockSum(c < 3 ? racc : 0.f, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    s = qBlockSum(c < 3 ? 0.f : racc, sh);
+    if (threadIdx.x == 0) partials[nb + blockIdx.x] = s;
+    s = qBlockSum(c < 3 ? xacc : 0.f, sh);
+    if (threadIdx.x == 0) partials[2 * nb + blockIdx.x] = s;
+    s = qBlockSum(c < 3 ? 0.f : xacc, sh);
+    if (threadIdx.x == 0) partials[3 * nb + blockIdx.x] = s;
 }
 
 // The residual is the anchor itself (x is the anchor state): r = r0 into rfloat (FP32) and rfull,
@@ -653,9 +696,18 @@ void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const
 
 void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
                            const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st) {
-    // nb partials per quantity: nb / 4 blocks per component
-    qk_step_start<<<dim3((unsigned)(nb / 4), 4), 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3,
-                                                               h.xo, h.wnew, h.w1, h.w2, rfloat, partials);
+    QStartRhs R{};
+    if (h.hx) {
+        R.hx = h.hx;
+        R.sg = h.sg;
+        R.sdt = h.sdt;
+        R.idt[0] = qdf(1.0 / (h.dt * g.dx));
+        R.idt[1] = qdf(1.0 / (h.dt * g.dy));
+        R.idt[2] = qdf(1.0 / (h.dt * g.dz));
+        R.x0 = h.x0;
+    }
+    qk_step_start<<<(unsigned)nb, 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3, h.xo, h.wnew,
+                                                 h.w1, h.w2, rfloat, partials, R);
 }
 
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st) {

@@ -42,8 +42,16 @@ struct QStepStart {
     qdf* wnew;                      // where w = D^-1 M (x_n - x_{n-1}) goes (null: not formed)
     const qdf* w1;                  // the stored w of the step before, and the one before that
     const qdf* w2;                  // (no two of x, xo*, wnew, w1, w2 alias)
+    // b - b_prev from x_n - x_{n-1} instead of two right-hand sides (hx: a copy of x_n; null:
+    // from b and bprev): the transient right-hand side's edge sigma and sigma / dt, dt, and x0,
+    // which receives x_n
+    const double* hx;
+    const double* sg;
+    const double* sdt;
+    double dt;
+    double* x0;
 };
-// nb (a multiple of 4): the blocks of the launch and the partials per quantity
+// nb: the blocks of the launch and the partials per quantity
 void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
                            const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st);
 // 1 / diag M as double-float (padded layout)

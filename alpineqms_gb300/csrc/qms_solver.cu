@@ -994,7 +994,7 @@ void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], boo
         // the step start (qk_step_start) formed this residual and its partials
         start_resid_ready = false;
         last_resid_df = true;
-        finalize(FIN_RESID, 4, start_nb());
+        finalize(FIN_RESID, 4, nbop);
         return;
     } else if (df_resid && anchor_ready && anchor_is_residual && !exact) {
         // x is the anchor state: the residual is the anchor's
@@ -1041,6 +1041,15 @@ void QmsSolver::resid_to_inner(T* out) {
     }
     qms_launch_pl_from_ref<T>(g, r64, S + S_INVNRM, out, st);
     nlaunch++;
+}
+
+// b of the last solve, formed from its start state (x0) when that solve took b - b_prev from
+// the state difference instead
+void QmsSolver::ensure_b() {
+    if (b_fresh) return;
+    qms_launch_rhs(g, ids, dtab64, last_ex, desc.dt, last_tr ? 1 : 0, x0, b, nullptr, st, rsg, rsdt);
+    nlaunch++;
+    b_fresh = true;
 }
 
 int QmsSolver::residual(bool adv, bool transient, const double v[3], bool exact) {
@@ -1151,24 +1160,36 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // Dirichlet values did not change over them
     const bool wcalc = chain && last_chained && wh[0];
     const bool start_fused = wcalc && xo > 0 && w_len >= xo - 1 && field_run >= xo + 2;
+    // with the field unchanged and x_(n-1) known, the anchor takes b - b_prev from x_n - x_(n-1)
+    // (the step start, in double-float) and this solve forms no FP64 right-hand side
+    const bool db_from_x = chain && same_field && hist_len >= 2 && hist_x && xold && rsg;
     start_resid_ready = false;
-    if (chain) {
+    if (chain && !db_from_x) {
+        ensure_b();                // b_prev: the last solve's right-hand side
         // x0 is copied, not swapped: the captured refinement graphs hold its address
         CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));   // the previous solution
         std::swap(b, bprev);
     }
-    // b from the previous solution (x); Dirichlet values written into x (warm start keeps them exact)
-    qms_launch_rhs(g, ids, dtab64, ex, desc.dt, transient ? 1 : 0, x, b, x, st, rsg, rsdt);
-    nlaunch++;
+    last_ex = ex;
+    last_tr = transient;
+    if (!db_from_x) {
+        // b from the previous solution (x); Dirichlet values written into x (warm start keeps them exact)
+        qms_launch_rhs(g, ids, dtab64, ex, desc.dt, transient ? 1 : 0, x, b, x, st, rsg, rsdt);
+        nlaunch++;
+        b_fresh = true;
+    } else {
+        b_fresh = false;           // formed from x0 when asked for (ensure_b)
+    }
     anchor_ready = false;          // the first residual of this solve is the FP64 anchor ...
     anchor_is_residual = false;
     if (chain) {                   // ... unless it follows from the previous one
         // the anchor, w_n and the extrapolated start in one pass; the residual of that start too
         // when start_fused (otherwise the double-float residual from the anchor follows)
         const int nw = std::min(desc.extrapolate, 3);          // w buffers: w_(n-1), w_(n-2), the new one
-        QStepStart hs{x, xold, xold2, xold3, xo, wcalc ? wh[nw - 1] : nullptr, wh[0], wh[1]};
+        QStepStart hs{x,       xold, xold2, xold3, xo, wcalc ? wh[nw - 1] : nullptr, wh[0], wh[1],
+                      db_from_x ? hist_x : nullptr, rsg, rsdt, desc.dt, db_from_x ? x0 : nullptr};
         OpEv* ev = start_fused ? prof_begin(3, (double)g.n * (8 * 11 + 8 * 2 * xo + 4)) : nullptr;
-        qms_launch_step_start(g, rfin, b, bprev, dinvdf, r0df, hs, start_fused ? rpl : nullptr, part, start_nb(), st);
+        qms_launch_step_start(g, rfin, b, bprev, dinvdf, r0df, hs, start_fused ? rpl : nullptr, part, nbop, st);
         nlaunch++;
         prof_end(ev);
         if (wcalc) {               // wh[0]: w_n, wh[1]: w_(n-1), the oldest becomes the next one's buffer
@@ -1344,6 +1365,8 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // A count that needed a third replay is not probed again for 32 solves.  (One longer cycle
     // in place of two does not pay: the FP32 inner solve stalls within a cycle, and a single
     // cycle needed ~23 steps where two of 7 sufficed.)
+    // (Probing below 6 steps where one replay finishes a solve, with a step back up after a
+    // solve that needed two, raised the count instead: a single slow step pins it for 32 solves.)
     if (graph_cycles > 0 && rel <= desc.tol) {
         if (gm_k_floor > 0 && ++gm_k_floor_age >= 32) { gm_k_floor--; gm_k_floor_age = 0; }
         if (graph_cycles >= 3) {

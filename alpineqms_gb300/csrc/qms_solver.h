@@ -80,9 +80,12 @@ struct QmsSolver {
     bool last_chained = false;  // the last solve's anchor state was the solution before it
     int field_run = 0;          // consecutive solves (this one included) with the same B, G
     bool start_resid_ready = false;   // the step start formed the first residual
-    // blocks of the step start's launch (and its partials per quantity): a multiple of 4 within
-    // the partial buffer's 4 nbop + 64
-    long long start_nb() const { return 4 * std::max(1LL, nbop / 4); }
+    // b holds the last solve's right-hand side (false: that solve took b - b_prev from x_n -
+    // x_(n-1); ensure_b forms it from x0, that solve's start state, and last_ex / last_tr)
+    bool b_fresh = false;
+    QmsExcite last_ex{};
+    bool last_tr = false;
+    void ensure_b();
     double* rsg = nullptr;      // edge sigma of every A row, and / dt (transient right-hand side)
     double* rsdt = nullptr;
     qdf* xdf = nullptr;         // x - x0

@@ -109,10 +109,11 @@ typedef struct {
     int mg_tail_points;      /* the coarse levels with at most this many points per block run their
                                 sub-cycle as one launch, one CTA per block (0: 4096; < 0: off) */
     int extrapolate;         /* a transient step that follows steps with the same operator starts
-                                from an extrapolation of the last solutions instead of x_n:
-                                2 (default) quadratic once three are known, 3 x_n - 3 x_(n-1) +
-                                x_(n-2) (linear before); 1 linear, 2 x_n - x_(n-1); 3 cubic once
-                                four are known, 4 x_n - 6 x_(n-1) + 4 x_(n-2) - x_(n-3); 0 none */
+                                from an extrapolation of the last solutions instead of x_n, of
+                                this order at most (lower while fewer solutions are known):
+                                3 (default) cubic, 4 x_n - 6 x_(n-1) + 4 x_(n-2) - x_(n-3);
+                                2 quadratic, 3 x_n - 3 x_(n-1) + x_(n-2); 1 linear,
+                                2 x_n - x_(n-1); 0 none */
 } qms_desc;
 
 typedef struct {

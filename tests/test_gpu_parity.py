@@ -362,9 +362,11 @@ def test_double_float_residual_agrees_with_fp64():
 def test_extrapolated_start_residual_by_linearity(order):
     """Once three steps in a row are chained, the residual of the extrapolated start follows from
     the anchor and the stored differences D^-1 M (x_n - x_(n-1)) of the last steps, without a
-    stencil pass (qk_step_start).  At the last step it must equal the exact FP64 residual of the
-    same start state (rebuilt here from the returned solutions), and every step must still reach
-    the tolerance with a final residual that agrees with the exact one."""
+    stencil pass, and the anchor takes b - b_prev from x_n - x_(n-1) (qk_step_start).  At the
+    last step the start residual must equal the exact FP64 residual of the same start state
+    (rebuilt here from the returned solutions), the right-hand side formed on demand must equal
+    the oracle's, and every step must reach the tolerance with a final residual that agrees with
+    the exact one."""
     p, geom = _conductor_case(True)
     from alpineqms_gb300.trajectory import VelocitySchedule
     from alpineqms_gb300.inputs import Trajectory
@@ -388,6 +390,12 @@ def test_extrapolated_start_residual_by_linearity(order):
         x_start = 3.0 * (X[-2] - X[-3]) + X[-4]
     else:
         x_start = 4.0 * (X[-2] + X[-4]) - 6.0 * X[-3] - X[-5]
+    # the chained steps took b - b_prev from the state difference: the last step's b, formed on
+    # demand from its start state, is still the reference's right-hand side bit for bit
+    c = o.materials(p["xs"], p["ys"], p["zs"], geom, p["props"])
+    _, _, _, br = o.assemble(p["xs"], p["ys"], p["zs"], p["dx"], p["dy"], p["dz"], c, True, p["dt"], v, B, G,
+                             x_prev=X[-2])
+    assert np.array_equal(s.get_rhs(), br)
     s.set_state(x_start)                 # b is still the last step's
     exact0 = s.residual_norm(True, v)
     s.close()
