@@ -34,6 +34,15 @@
 
 namespace {
 
+// (i, j, k) of offset q in a block of n1 x n2 x n3 points, in 32-bit arithmetic (a block of a
+// level holds far fewer than 2^32 points)
+__device__ __forceinline__ void mg_ijk(long long q, int n1, int n2, int& i, int& j, int& k) {
+    const unsigned u = (unsigned)q, a = u / (unsigned)n1, c = a / (unsigned)n2;
+    i = (int)(u - a * (unsigned)n1);
+    j = (int)(a - c * (unsigned)n2);
+    k = (int)c;
+}
+
 template <typename T>
 __device__ __forceinline__ int find_block(const MGLevelDev<T>& L, long long t) {
     int b = 0;
@@ -104,7 +113,8 @@ template <typename T, typename Fine, typename Act>
 __device__ __forceinline__ void mg_coarsen_point(const MGBlockDesc& fb, const MGBlockDesc& cb, int b, long long t,
                                                  MGLevelDev<T>& C, Fine fine, Act act) {
     long long q = t - cb.off;
-    const int I = (int)(q % cb.n1), J = (int)((q / cb.n1) % cb.n2), K = (int)(q / ((long long)cb.n1 * cb.n2));
+    int I, J, K;
+    mg_ijk(q, cb.n1, cb.n2, I, J, K);
     double d = 0.0, w1 = 0.0, w2 = 0.0, w3 = 0.0;
     bool any = false;
     const long long s2 = fb.n1, s3 = (long long)fb.n1 * fb.n2;
@@ -172,7 +182,8 @@ __global__ void mg_mask_links(MGLevelDev<T> C) {
     const int b = find_block(C, t);
     const MGBlockDesc& cb = C.blk[b];
     long long q = t - cb.off;
-    const int I = (int)(q % cb.n1), J = (int)((q / cb.n1) % cb.n2), K = (int)(q / ((long long)cb.n1 * cb.n2));
+    int I, J, K;
+    mg_ijk(q, cb.n1, cb.n2, I, J, K);
     if (C.dinv[t] == T(0)) { C.w1[t] = C.w2[t] = C.w3[t] = T(0); return; }
     if (I + 1 < cb.n1 && C.dinv[t + 1] == T(0)) C.w1[t] = T(0);
     if (J + 1 < cb.n2 && C.dinv[t + cb.n1] == T(0)) C.w2[t] = T(0);
@@ -220,7 +231,8 @@ __global__ void mg_smooth(MGLevelDev<T> L, const T* __restrict__ b, const float*
     const int bk = find_block(L, t);
     const MGBlockDesc& B = L.blk[bk];
     long long q = t - B.off;
-    const int i = (int)(q % B.n1), j = (int)((q / B.n1) % B.n2), k = (int)(q / ((long long)B.n1 * B.n2));
+    int i, j, k;
+    mg_ijk(q, B.n1, B.n2, i, j, k);
     T bv = b[t];
     if (bscale) bv *= (T)bscale[t];
     xout[t] = xin[t] + omega * di * (bv - apply7(L, B, t, i, j, k, xin));
@@ -236,7 +248,8 @@ __global__ void mg_restrict(MGLevelDev<T> F, const T* __restrict__ bf, const flo
     const MGBlockDesc& cb = C.blk[b];
     const MGBlockDesc& fb = F.blk[b];
     long long q = t - cb.off;
-    const int I = (int)(q % cb.n1), J = (int)((q / cb.n1) % cb.n2), K = (int)(q / ((long long)cb.n1 * cb.n2));
+    int I, J, K;
+    mg_ijk(q, cb.n1, cb.n2, I, J, K);
     T acc = T(0);
     if (!(mask_v && b == C.nb - 1)) {
         for (int dk = 0; dk < 2; dk++) for (int dj = 0; dj < 2; dj++) for (int di = 0; di < 2; di++) {
@@ -262,7 +275,8 @@ __global__ void mg_prolong(MGLevelDev<T> F, const T* xin, T* xf, MGLevelDev<T> C
     const MGBlockDesc& fb = F.blk[b];
     const MGBlockDesc& cb = C.blk[b];
     long long q = t - fb.off;
-    const int i = (int)(q % fb.n1), j = (int)((q / fb.n1) % fb.n2), k = (int)(q / ((long long)fb.n1 * fb.n2));
+    int i, j, k;
+    mg_ijk(q, fb.n1, fb.n2, i, j, k);
     xf[t] = xin[t] + alpha * xc[cb.off + (i >> 1) + (long long)(j >> 1) * cb.n1 + (long long)(k >> 1) * cb.n1 * cb.n2];
 }
 
@@ -312,7 +326,8 @@ __global__ void __launch_bounds__(1024) mg_tail(MGTail<T> tl, const double* __re
             const long long t = B.off + q;
             const T di = masked ? T(0) : L.dinv[t];
             if (di == T(0)) { xout[t] = T(0); continue; }
-            const int i = (int)(q % B.n1), j = (int)((q / B.n1) % B.n2), k = (int)(q / ((long long)B.n1 * B.n2));
+            int i, j, k;
+            mg_ijk(q, B.n1, B.n2, i, j, k);
             xout[t] = xin[t] + omega * di * (L.b[t] - apply7(L, B, t, i, j, k, xin));
         }
         __syncthreads();
@@ -340,7 +355,8 @@ __global__ void __launch_bounds__(1024) mg_tail(MGTail<T> tl, const double* __re
         const MGBlockDesc& cb = C.blk[b];
         const long long nc = npts(cb);
         for (long long q = threadIdx.x; q < nc; q += blockDim.x) {
-            const int I = (int)(q % cb.n1), J = (int)((q / cb.n1) % cb.n2), K = (int)(q / ((long long)cb.n1 * cb.n2));
+            int I, J, K;
+            mg_ijk(q, cb.n1, cb.n2, I, J, K);
             T acc = T(0);
             if (!masked)
                 for (int dk = 0; dk < 2; dk++) for (int dj = 0; dj < 2; dj++) for (int dd = 0; dd < 2; dd++) {
@@ -380,7 +396,8 @@ __global__ void __launch_bounds__(1024) mg_tail(MGTail<T> tl, const double* __re
         for (long long q = threadIdx.x; q < n; q += blockDim.x) {
             const long long p = B.off + q;
             if (L.dinv[p] == T(0) || masked) { x[p] = T(0); continue; }
-            const int i = (int)(q % B.n1), j = (int)((q / B.n1) % B.n2), k = (int)(q / ((long long)B.n1 * B.n2));
+            int i, j, k;
+            mg_ijk(q, B.n1, B.n2, i, j, k);
             x[p] += alpha * xc[cb.off + (i >> 1) + (long long)(j >> 1) * cb.n1 + (long long)(k >> 1) * cb.n1 * cb.n2];
         }
         __syncthreads();

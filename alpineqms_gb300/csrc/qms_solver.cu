@@ -1101,6 +1101,7 @@ int QmsSolver::ir_iteration_graph(bool adv, bool transient, const double v[3], i
             int it = 0;
             rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it, k) : inner_gmres<float>(adv, transient, v, it, k);
             residual_launch(adv, transient, v);
+            G->resid_df = last_resid_df;
         }
         cudaGraph_t graph = nullptr;
         if (e == cudaSuccess) e = cudaStreamEndCapture(st, &graph);
@@ -1127,6 +1128,8 @@ int QmsSolver::ir_iteration_graph(bool adv, bool transient, const double v[3], i
     G->used = ++graph_clock;
     CK(cudaGraphLaunch(G->exec, st));
     nlaunch += G->launches;
+    // host state that the captured residual sets: a replay ends in the same kind of residual
+    last_resid_df = G->resid_df;
     last_inner = 2;
     last_gm_k = k;
     int rc = read_scalars();                     // synchronises the stream

@@ -160,6 +160,7 @@ struct QmsSolver {
         cudaGraphExec_t exec = nullptr;
         int k = 0;
         bool tr = false, adv = false, prof = false;
+        bool resid_df = false;      // the captured residual is the double-float one (rfin)
         double v[3] = {0, 0, 0};
         long long launches = 0;
         std::vector<OpEv> ev;
