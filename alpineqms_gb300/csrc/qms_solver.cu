@@ -238,12 +238,14 @@ template <> struct GmPack<double> {
     static __device__ __forceinline__ double at(const V& v, int q) { return q == 0 ? v.x : v.y; }
 };
 
+// h_ij = V_i . w for i < NV, and w . w (partials at NV nb + block)
 template <typename T, int NV>
 __global__ void __launch_bounds__(256) qk_gm_dots(long long n, GmPtrs V, const T* __restrict__ w,
                                                   double* __restrict__ part) {
     using PK = GmPack<T>;
     using PV = typename PK::V;
     float acc[NV];
+    float accw = 0.f;
 #pragma unroll
     for (int i = 0; i < NV; i++) acc[i] = 0.f;
     const PV* vp[NV];
@@ -260,6 +262,8 @@ __global__ void __launch_bounds__(256) qk_gm_dots(long long n, GmPtrs V, const T
         for (int i = 0; i < NV; i++)
 #pragma unroll
             for (int q = 0; q < PK::W; q++) acc[i] += (float)(PK::at(vv[i], q) * PK::at(wv, q));
+#pragma unroll
+        for (int q = 0; q < PK::W; q++) accw += (float)(PK::at(wv, q) * PK::at(wv, q));
     }
     __shared__ double sh[32];
 #pragma unroll
@@ -267,30 +271,52 @@ __global__ void __launch_bounds__(256) qk_gm_dots(long long n, GmPtrs V, const T
         double sum = qBlockSum(acc[i], sh);
         if (threadIdx.x == 0) part[(long long)i * gridDim.x + blockIdx.x] = sum;
     }
+    const double sw = qBlockSum(accw, sh);
+    if (threadIdx.x == 0) part[(long long)NV * gridDim.x + blockIdx.x] = sw;
 }
 
-// column j of H from the partials (h_ij = V_i . w)
-__global__ void qk_gm_hcol(const double* __restrict__ part, long long nb, int j, int m, double* __restrict__ Hm) {
+// column j of H from the partials (h_ij = V_i . w), and the norm of the orthogonalised w from
+// Pythagoras, |w'|^2 = |w|^2 - sum_i h_ij^2: when that keeps at least a hundredth of |w|^2 (no
+// severe cancellation), Gm[4] = |w'| and Gm[3] = 1, and the orthogonalisation writes V_{j+1}
+// = w' / |w'| directly (no norm pass over w', no scaling pass); otherwise Gm[3] = 0
+__global__ void qk_gm_hcol(const double* __restrict__ part, long long nb, int j, int m, double* __restrict__ Hm,
+                           double* __restrict__ Gm) {
     __shared__ double sh[32];
-    for (int i = 0; i <= j; i++) {
+    double hh = 0.0;
+    for (int i = 0; i <= j + 1; i++) {
         double acc = 0.0;
         for (long long t = threadIdx.x; t < nb; t += blockDim.x) acc += part[(long long)i * nb + t];
         double s = qBlockSum(acc, sh);
-        if (threadIdx.x == 0) Hm[i * m + j] = s;
+        if (threadIdx.x == 0) {
+            if (i <= j) {
+                Hm[i * m + j] = s;
+                hh += s * s;
+            } else {
+                const double est = s - hh;
+                const bool ok = isfinite(est) && est > 1e-2 * s;
+                Gm[3] = ok ? 1.0 : 0.0;
+                Gm[4] = ok ? sqrt(est) : 0.0;
+            }
+        }
     }
 }
 
-// w -= sum_i h_ij V_i ; partials of |w|^2   (NV = j + 1, compile-time; 16-byte packets)
+// w' = w - sum_i h_ij V_i (NV = j + 1, compile-time; 16-byte packets): with Gm[3] set, V_{j+1} =
+// w' / Gm[4] goes to vout; otherwise w' back into w with the partials of |w'|^2
 template <typename T, int NV>
 __global__ void __launch_bounds__(256) qk_gm_orth(long long n, int j, int m, GmPtrs V, const double* __restrict__ Hm,
-                                                  T* __restrict__ w, double* __restrict__ part) {
+                                                  T* __restrict__ w, double* __restrict__ part,
+                                                  const double* __restrict__ Gm, T* __restrict__ vout) {
     using PK = GmPack<T>;
     using PV = typename PK::V;
     T h[NV];
     const PV* vp[NV];
 #pragma unroll
     for (int i = 0; i < NV; i++) { h[i] = (T)Hm[i * m + j]; vp[i] = (const PV*)V.p[i]; }
+    const bool direct = Gm[3] != 0.0;
+    const T inv = direct ? (T)(1.0 / Gm[4]) : T(1);
     PV* wp = (PV*)w;
+    PV* op = direct ? (PV*)vout : wp;
     const long long np = n / PK::W;
     float acc = 0.f;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < np; t += (long long)gridDim.x * blockDim.x) {
@@ -304,11 +330,12 @@ __global__ void __launch_bounds__(256) qk_gm_orth(long long n, int j, int m, GmP
             T a = wq[q];
 #pragma unroll
             for (int i = 0; i < NV; i++) a -= h[i] * PK::at(vv[i], q);
-            wq[q] = a;
+            wq[q] = direct ? a * inv : a;
             acc += (float)(a * a);
         }
-        wp[t] = wv;
+        op[t] = wv;
     }
+    if (direct) return;
     __shared__ double sh[32];
     double s0 = qBlockSum(acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = s0;
@@ -319,11 +346,13 @@ __global__ void __launch_bounds__(256) qk_gm_orth(long long n, int j, int m, GmP
 __global__ void qk_gm_givens(const double* __restrict__ part, long long nb, int j, int m, double* __restrict__ Hm,
                              double* __restrict__ Gm, unsigned* __restrict__ status) {
     __shared__ double sh[32];
+    const bool direct = Gm[3] != 0.0;
     double acc = 0.0;
-    for (long long t = threadIdx.x; t < nb; t += blockDim.x) acc += part[t];
+    if (!direct)
+        for (long long t = threadIdx.x; t < nb; t += blockDim.x) acc += part[t];
     double nw = qBlockSum(acc, sh);
     if (threadIdx.x != 0) return;
-    double hn = sqrt(nw);
+    double hn = direct ? Gm[4] : sqrt(nw);
     double* cs = Gm + 8;
     double* sn = Gm + 8 + m;
     double* gv = Gm + 8 + 2 * m;
@@ -344,9 +373,10 @@ __global__ void qk_gm_givens(const double* __restrict__ part, long long nb, int 
     if (!(r > 0.0) || !isfinite(r)) atomicOr(status, (unsigned)QMS_ST_BREAKDOWN);
 }
 
-// V_{j+1} = w / h_{j+1,j}
+// V_{j+1} = w / h_{j+1,j} (nothing to do when the orthogonalisation wrote it, Gm[3])
 template <typename T>
 __global__ void qk_gm_scale(long long n, const T* __restrict__ w, T* __restrict__ vout, const double* __restrict__ Gm) {
+    if (Gm[3] != 0.0) return;
     const T inv = (T)Gm[2];
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
         vout[t] = w[t] * inv;
@@ -414,9 +444,9 @@ static void gm_dots(int nv, int vb, cudaStream_t st, long long n, const GmPtrs& 
 }
 template <typename T>
 static void gm_orth(int nv, int vb, cudaStream_t st, long long n, int j, int m, const GmPtrs& V, const double* Hm, T* w,
-                    double* part) {
+                    double* part, const double* Gm, T* vout) {
     switch (nv) {
-#define C(N) case N: qk_gm_orth<T, N><<<vb, 256, 0, st>>>(n, j, m, V, Hm, w, part); break;
+#define C(N) case N: qk_gm_orth<T, N><<<vb, 256, 0, st>>>(n, j, m, V, Hm, w, part, Gm, vout); break;
         GM_CASES(C)
 #undef C
     }
@@ -926,8 +956,8 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
         if (use_mg) precond<T>(vj, dg, zj, false, transient, false, &P, adv);
         op_pl<T>(adv, QOPH_SCALED, P, zj, w, nullptr, nullptr);
         gm_dots<T>(j + 1, vb, st, n, Vp, w, part);
-        qk_gm_hcol<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H);
-        gm_orth<T>(j + 1, vb, st, n, j, m, Vp, gm_H, w, part);
+        qk_gm_hcol<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H, gm_scal);
+        gm_orth<T>(j + 1, vb, st, n, j, m, Vp, gm_H, w, part, gm_scal, (T*)gmV[j + 1]);
         qk_gm_givens<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H, gm_scal, status);
         qk_gm_scale<T><<<vb, 256, 0, st>>>(n, w, (T*)gmV[j + 1], gm_scal);
         nlaunch += 5;
