@@ -1175,7 +1175,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     for (int q = 0; q < 3; q++) { ex.B[q] = B[q]; ex.v[q] = v[q]; }
     for (int q = 0; q < 9; q++) ex.G[q] = G[q];
     // the previous solve's final residual anchors this one when the operator is the same
-    const bool chain = df_resid && transient && rfin_ok && chain_len < 16 && chain_v[0] == v[0] &&
+    const bool chain = df_resid && transient && rfin_ok && chain_len < QMS_CHAIN_MAX && chain_v[0] == v[0] &&
                        chain_v[1] == v[1] && chain_v[2] == v[2];
     // the start of a transient solve that follows solves with the same operator: an extrapolation
     // of the last solutions (x = hist[0], the one before in hist[1], ...), independent of how the
@@ -1398,8 +1398,9 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // A count that needed a third replay is not probed again for 32 solves.  (One longer cycle
     // in place of two does not pay: the FP32 inner solve stalls within a cycle, and a single
     // cycle needed ~23 steps where two of 7 sufficed.)
-    // (Probing below 6 steps where one replay finishes a solve, with a step back up after a
-    // solve that needed two, raised the count instead: a single slow step pins it for 32 solves.)
+    // One-replay solves probe down to 5 steps; a probe below 6 that needed a second replay goes
+    // back to 6, which then holds for 32 solves.  (Letting any count step back up after a
+    // second replay raised it instead: one slow step pinned it at 7-8 for 32 solves.)
     if (graph_cycles > 0 && rel <= desc.tol) {
         if (gm_k_floor > 0 && ++gm_k_floor_age >= 32) { gm_k_floor--; gm_k_floor_age = 0; }
         if (graph_cycles >= 3) {
@@ -1408,11 +1409,16 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
             gm_k_est = std::min(gm_m, gm_k_est + 2);
             gm_k_fine = true;
         } else if (graph_cycles == 2 && gm_cycles == 2) {
-            if (rel < desc.tol / 3.0)
+            if (gm_k_est < 6) {
+                gm_k_est = 6;
+                gm_k_floor = 6;
+                gm_k_floor_age = 0;
+            } else if (rel < desc.tol / 3.0) {
                 gm_k_est = std::max(std::max(6, gm_k_floor),
                                     gm_k_est - (gm_k_fine ? 1 : std::max(1, gm_k_est / 5)));
+            }
         } else if (graph_cycles == 1 && gm_cycles == 1 && rel < desc.tol / 3.0) {
-            gm_k_est = std::max(std::max(6, gm_k_floor), gm_k_est - 1);
+            gm_k_est = std::max(std::max(5, gm_k_floor), gm_k_est - 1);
         }
     }
     unsigned stt = 0;

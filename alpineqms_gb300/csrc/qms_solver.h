@@ -15,6 +15,9 @@
 
 size_t qms_device_bytes_impl(const qms_desc& d);
 
+// transient steps chained to an anchor before an exact FP64 one is taken again
+#define QMS_CHAIN_MAX 32
+
 struct QmsSolver {
     qms_desc desc{};
     QGrid g{};
@@ -57,7 +60,9 @@ struct QmsSolver {
     double* x0 = nullptr;
     // Chained anchor: a transient solve with the operator of the previous one starts from that
     // solve's final residual, r0 = r_fin + D^-1 (b - b_prev), instead of an FP64 residual (an
-    // exact one every 16 steps, and whenever the operator or the state changed otherwise).
+    // exact one after QMS_CHAIN_MAX chained steps, and whenever the operator or the state changed
+    // otherwise).  Each chained step adds the double-float rounding of one residual (~1e-16 of
+    // |x|) to the anchor; the drift test runs a full chain against the FP64 residual.
     double* bprev = nullptr;    // right-hand side of the previous solve
     qdf* rfin = nullptr;        // the last double-float residual, in full
     qdf* dinvdf = nullptr;      // 1 / diag M of the transient operator

@@ -358,6 +358,33 @@ def test_double_float_residual_agrees_with_fp64():
 
 
 @pytest.mark.gpu
+def test_chained_residual_does_not_drift():
+    """A transient run chains each step's anchor to the previous step's final double-float
+    residual for up to 32 steps.  Over 40 steps with one operator (a full chain, a re-anchor and
+    the start of the next chain) every step's final residual must agree with the exact FP64
+    residual of the returned state to a tenth of the tolerance."""
+    p, geom = _conductor_case(True)
+    from alpineqms_gb300.trajectory import VelocitySchedule
+    from alpineqms_gb300.inputs import Trajectory
+    sched = VelocitySchedule([Trajectory(1, *t) for t in p["traj"]], p["dt"])
+    s = solver_for(p["xs"], p["ys"], p["zs"], (p["dx"], p["dy"], p["dz"]), p["dt"], geom, p["props"],
+                   precision="mixed")
+    tol = s.desc.tol
+    B, G = np.asarray(p["B"], np.float64), np.asarray(p["G"], np.float64).ravel()
+    s.steady(sched.steady(), B, G)
+    v = sched.step(1)
+    worst = 0.0
+    for n in range(1, 41):
+        st = s.step(v, B, G)
+        assert st["status"] == 0, (n, st)
+        exact = s.residual_norm(True, v)
+        assert exact <= tol * 1.5, (n, exact)
+        worst = max(worst, abs(st["r"] - exact))
+    s.close()
+    assert worst <= 0.1 * tol, worst
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("order", [1, 2, 3])
 def test_extrapolated_start_residual_by_linearity(order):
     """Once three steps in a row are chained, the residual of the extrapolated start follows from
