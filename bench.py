@@ -5,7 +5,7 @@ Workload (default): the 256^3 moving-conductor case (aluminium plate
 200x200x10, sigma 3.5e7 S/m, in Bz = 10 mT + 0.1 T/m z-gradient; the frame
 ramps to -10 m/s along x in the first step; dt = 1e-5 s).  n_dims =
 67,700,225 unknowns (~50.7 M edge A + ~17 M node V).  A "step" is one
-backward-Euler step: RHS build, FP64-refined solve to ||D^-1 r|| <= 1e-12 ||x||.
+backward-Euler step: RHS, FP64-refined solve to ||D^-1 r|| <= 2e-13 ||x||.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
     python bench.py --impl reference ...     # the reference algorithm on the host cores
@@ -14,8 +14,9 @@ value   = n_dims * K / (device time of K steps), inputs resident in HBM.
 e2e     = the same metric through the public Python API per step (qms_step
           with the step's velocity/field from host memory + read-back of the
           H slice the reference dumps every step).
-roofline: the dominant kernel (matrix-free FP32 operator or FP64 residual),
-          algorithmic bytes / CUDA-event time of its launches in the timed region.
+roofline: the inner solver's matrix-free FP32 operator: algorithmic bytes / CUDA-event
+          time of its launches in a second pass of as many steps with the profile's
+          events on (the timed pass runs without them).
 cpu_baseline: the CPU oracle (C restatement of the reference assembly with
           OpenMP + SuperLU direct solve reused across steps, as PARDISO phase 33)
           on a bounded sample: the same workload at a reduced grid.
