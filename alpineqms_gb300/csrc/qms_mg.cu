@@ -423,6 +423,9 @@ __global__ void __launch_bounds__(1024) mg_tail(MGTail<T> tl, const double* __re
 // of stored per-point links:
 //   KIND 0: x = omega D^-1 b                      (first sweep, zero guess)
 //   KIND 1: x_out = x_in + omega D^-1 (b - A x_in)
+//   KIND 3: the first two sweeps from a zero guess in one pass (scaled b only): the
+//           first sweep is x_1 = omega isc b pointwise (the diagonal cancels against
+//           the row scaling), so b's tile is staged in x_in's place and scaled on use
 //   KIND 2: b_c = sum over each 2x2x2 aggregate of (b - A x_in)  (restriction
 //           fused with the residual; pairs in i via lane shuffles, in j via
 //           shared memory, in k in registers -- no atomics, fixed order)
@@ -560,12 +563,15 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
                 xout[row] = omega * bv * mg_rcp(d);
                 return;
             }
-            const T xc = XS(q, x0, 0, 0);
+            const T xs = XS(q, x0, 0, 0);
             // difference form (rounding scales with the variation of x): d - sum(w) is the mass
             // term, or the diagonal shift of V
-            const T Ax = wxp * (xc - XS(q, x0, 0, 1)) + wxm * (xc - XS(q, x0, 0, -1)) + wyp * (xc - XS(q, x0, 1, 0)) +
-                         wym * (xc - XS(q, x0, -1, 0)) + wzp * (xc - XS(q, xp, 0, 0)) + wzm * (xc - XS(q, xm, 0, 0)) +
-                         (dextra * dscale + (wxp + wxm + wyp + wym + wzp + wzm) * (dscale - T(1))) * xc;
+            const T Axs = wxp * (xs - XS(q, x0, 0, 1)) + wxm * (xs - XS(q, x0, 0, -1)) + wyp * (xs - XS(q, x0, 1, 0)) +
+                          wym * (xs - XS(q, x0, -1, 0)) + wzp * (xs - XS(q, xp, 0, 0)) + wzm * (xs - XS(q, xm, 0, 0)) +
+                          (dextra * dscale + (wxp + wxm + wyp + wym + wzp + wzm) * (dscale - T(1))) * xs;
+            // KIND 3: the staged values are b; x_1 = c b with c = omega isc, and A x_1 = c A b
+            const T cq = KIND == 3 ? omega * isc : T(1);
+            const T xc = cq * xs, Ax = cq * Axs;
             if (KIND == 2) r[q - S::Q0] = bv - Ax;
             else xout[row] = xc + omega * (bv - Ax) * mg_rcp(d);
         };
@@ -664,8 +670,8 @@ static void mg0_prepare() {
 #define ATTR(K, Q) \
     cudaFuncSetAttribute(mg0_tiled<T, K, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mg0_smem<T, K, Q>())
     ATTR(0, 0); ATTR(1, 0); ATTR(2, 0);
-    ATTR(0, 1); ATTR(1, 1); ATTR(2, 1);
-    ATTR(0, 2); ATTR(1, 2); ATTR(2, 2);
+    ATTR(0, 1); ATTR(1, 1); ATTR(2, 1); ATTR(3, 1);
+    ATTR(0, 2); ATTR(1, 2); ATTR(2, 2); ATTR(3, 2);
 #undef ATTR
     done.fetch_or(bit, std::memory_order_acq_rel);
 }
@@ -945,16 +951,18 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
 // result in x0; t0 is a level-0 temporary.  Returns the number of kernel launches.
 template <typename T>
 int QmsMG<T>::vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
-                     const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st, int qs) {
-    if (qs == 1) return vcycle_q<1>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st);
-    if (qs == 2) return vcycle_q<2>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st);
-    return vcycle_q<0>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st);
+                     const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st, int qs,
+                     const CUtensorMap* b0map) {
+    if (qs == 1) return vcycle_q<1>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st, b0map);
+    if (qs == 2) return vcycle_q<2>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st, b0map);
+    return vcycle_q<0>(b0, scaled, x0, x0map, t0, t0map, cmap, mask_v, err, st, nullptr);
 }
 
 template <typename T>
 template <int QS>
 int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
-                       const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st) {
+                       const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st,
+                       const CUtensorMap* b0map) {
     int launches = 0;
     std::vector<MGLevelDev<T>>& lv = QS == 0 ? this->lv : views[QS];   // levels >= 1 of the cycle's blocks
     const long long* dmo = dmoff + (QS == 2 ? 3 : 0);                    // their dense coarsest inverses
@@ -975,9 +983,20 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     // start in t0 when that count is even so that the last write lands in x0
     Buf x{x0, &x0map}, t{t0, &t0map};
     if ((n1 + n2) % 2 == 0) std::swap(x, t);
-    MG0(0, x, x.p, nullptr);
-    launches++;
-    for (int s = 1; s < n1; s++) {
+    int s = 1;
+    if (b0map && scaled && QS != 0 && n1 >= 2) {
+        // the first two sweeps in one pass, from b's tiles (KIND 3), into the buffer the second
+        // sweep writes
+        Buf bb{const_cast<T*>(b0), b0map};
+        MG0(3, bb, t.p, nullptr);
+        std::swap(x, t);
+        launches++;
+        s = 2;
+    } else {
+        MG0(0, x, x.p, nullptr);
+        launches++;
+    }
+    for (; s < n1; s++) {
         MG0(1, x, t.p, nullptr);
         std::swap(x, t);
         launches++;

@@ -63,11 +63,14 @@ struct QmsMG {
     // result, t0 a temporary; the tensor maps of x0, t0 and of the node coefficients
     // qs: 0 all blocks, 1 the A blocks only, 2 the V block only (x0map / t0map then cover those
     // blocks, cmap the node coefficients they read: all six, or the three conductivities)
+    // b0map (qs 1 or 2, scaled): b0's tensor map over the cycle's blocks; the first two level-0
+    // sweeps then run as one pass from b0's tiles
     int vcycle(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
-               const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st, int qs = 0);
+               const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st, int qs = 0,
+               const CUtensorMap* b0map = nullptr);
     template <int QS>
     int vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map, T* t0, const CUtensorMap& t0map,
-                 const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st);
+                 const CUtensorMap& cmap, bool mask_v, unsigned* err, cudaStream_t st, const CUtensorMap* b0map);
     static int levels_for(const QGrid& g, int min_coarse);
 };
 

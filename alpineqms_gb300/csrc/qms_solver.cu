@@ -851,9 +851,16 @@ void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool
         const bool f32 = sizeof(T) == 4;
         const CUtensorMap& cm = f32 ? cmap32 : cmap64;
         auto cycle = [&](const T* b, int qs, const CUtensorMap& cmq) {
+            // b's own tile map for the fused first sweeps of the subset cycles (a mapped vector)
+            const CUtensorMap* bm = nullptr;
+            if (qs != 0) {
+                auto& tm = qs == 1 ? tmapsA : tmapsV;
+                auto it = tm.find((const void*)b);
+                if (it != tm.end()) bm = &it->second;
+            }
             if (f32)
                 nlaunch += mgf[transient ? 1 : 0].vcycle((const float*)b, bscale != nullptr, (float*)z, tmapq(z, qs),
-                                                         mgtmp, tmapq(mgtmp, qs), cmq, mask_v, status, st, qs);
+                                                         mgtmp, tmapq(mgtmp, qs), cmq, mask_v, status, st, qs, bm);
             else
                 nlaunch += mgd[transient ? 1 : 0].vcycle((const double*)b, bscale != nullptr, (double*)z,
                                                          tmapq(z, qs), (double*)mgtmp, tmapq(mgtmp, qs), cmq, mask_v,
