@@ -10,6 +10,12 @@
 // Addition is the "sloppy" double-word sum: its absolute error is a few units of 2^-48 of
 // the larger operand, which is what a residual of difference-form rows needs.  Products follow
 // the double-word times double-word scheme of Joldes, Muller and Popescu (ACM TOMS 44, 2017).
+// Products return the pair without the final renormalisation (fast_two_sum): the high word is
+// the float product and the low word gathers the rounding error and the cross terms, so |l|
+// may reach a few units of ulp(h) instead of ulp(h) / 2 -- a product never cancels, so h still
+// carries the value, and the next sum or product takes such a pair as it is.  Sums stay
+// renormalised: a difference can cancel its high words, and a product of an unnormalised
+// difference would lose the low word's cross term.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -53,9 +59,7 @@ __device__ __forceinline__ qdf operator*(qdf x, qdf y) {
     float e = __fmaf_rn(x.h, y.h, -p);
     e = __fmaf_rn(x.h, y.l, e);
     e = __fmaf_rn(x.l, y.h, e);
-    qdf r;
-    qdf_fast_two_sum(p, e, r.h, r.l);
-    return r;
+    return qdf(p, e);
 }
 // x / y: a float quotient, corrected once with the double-float remainder x - q y
 __device__ __forceinline__ qdf operator/(qdf x, qdf y) {
