@@ -279,24 +279,6 @@ __global__ void qk_extrapolate(QGrid g, double* __restrict__ x, const double* __
     if (!qFixV(g, i, j, k)) one(qV(g, i, j, k));
 }
 
-// r0 = rprev + D^-1 (b - bprev): the residual of the previous solution against the new
-// right-hand side, from the previous solve's final residual (the operator is unchanged)
-__global__ void qk_chain_anchor(QGrid g, const qdf* __restrict__ rprev, const double* __restrict__ b,
-                                const double* __restrict__ bprev, const qdf* __restrict__ dinv, qdf* __restrict__ r0) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > g.Nx || j > g.Ny) return;
-    const QPL L = qms_pl(g);
-    const long long t = qms_pl_node(g, L, i, j, k);
-    auto one = [&](long long ref, long long pl) {
-        r0[pl] = rprev[pl] + qdf_split(b[ref] - bprev[ref]) * dinv[pl];
-    };
-    if (i <= g.xs) one(qAX(g, i, j, k), t);
-    if (j <= g.ys) one(qAY(g, i, j, k), L.comp + t);
-    if (k <= g.zs) one(qAZ(g, i, j, k), 2 * L.comp + t);
-    one(qV(g, i, j, k), 3 * L.comp + t);
-}
-
 // The start of a transient step chained to the previous one, in one pass over the unknowns:
 //   r0 = rfin + D^-1 (b - b_prev)      the anchor: the residual of x_n, the previous solution,
 //                                      against the new right-hand side
@@ -714,10 +696,6 @@ void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<d
     qk_dinv_df<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, c, P, out);
 }
 
-void qms_launch_chain_anchor(const QGrid& g, const qdf* rprev, const double* b, const double* bprev, const qdf* dinv,
-                             qdf* r0, cudaStream_t st) {
-    qk_chain_anchor<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, rprev, b, bprev, dinv, r0);
-}
 
 void qms_launch_pl_scale(long long n, const float* r, const double* scale, float* out, cudaStream_t st) {
     qk_pl_scale<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 16), 256, 0, st>>>(n, r, scale, out);

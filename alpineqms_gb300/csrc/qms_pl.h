@@ -56,9 +56,6 @@ void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const dou
                            const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st);
 // 1 / diag M as double-float (padded layout)
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st);
-// r0 = rprev + D^-1 (b - bprev)   (b, bprev in reference order; the rest padded, double-float)
-void qms_launch_chain_anchor(const QGrid& g, const qdf* rprev, const double* b, const double* bprev, const qdf* dinv,
-                             qdf* r0, cudaStream_t st);
 // dx = x - x0 as double-float (padded layout) and the partials |x_A|^2, |x_V|^2 of nb blocks
 void qms_launch_delta_split(const QGrid& g, const double* x, const double* x0, qdf* dx, double* partials,
                             long long nb, cudaStream_t st);
