@@ -99,3 +99,15 @@ def test_struct_layouts_match_header(tmp_path):
         assert got[(name, "size")] == ctypes.sizeof(ct), name
         for fname, _ in ct._fields_:
             assert got[(name, fname)] == getattr(ct, fname).offset, (name, fname)
+
+
+def test_default_descriptor(lib):
+    """qms_default_desc (host-only) fills the documented defaults of the solver."""
+    from alpineqms_gb300._lib import QmsDesc
+    d = QmsDesc()
+    lib.qms_default_desc(ctypes.byref(d), 64, 48, 32, 1e-3, 2e-3, 3e-3, 1e-5)
+    assert (d.xs, d.ys, d.zs) == (64, 48, 32)
+    assert (d.dx, d.dy, d.dz, d.dt) == (1e-3, 2e-3, 3e-3, 1e-5)
+    assert d.tol == 2e-13 and d.gmres_m == 32 and d.max_outer == 60
+    assert d.mg_sweeps == 3 and d.mg_omega == 0.85 and d.mg_alpha == 1.5
+    assert d.mg_coupling == 1 and d.extrapolate == 3
