@@ -157,7 +157,10 @@ int qms_get_fields(qms_handle* h, int which, int axis, int index, double* out);
 int qms_get_state(qms_handle* h, double* x_out);          /* n_dims doubles */
 int qms_get_rhs(qms_handle* h, double* b_out);            /* n_dims doubles: the right-hand side of the last
                                                              solve (RHS of F:1457-2191, Dirichlet values
-                                                             in their rows) */
+                                                             in their rows), bit-exact; a chained transient
+                                                             step with an unchanged field does not form it,
+                                                             and this call then forms it from that step's
+                                                             start state */
 int qms_set_state(qms_handle* h, const double* x_in);
 
 /* Verification path: CSR of the steady (transient = 0) or transient system and
