@@ -133,6 +133,7 @@ SIGNATURES = [
     ("qms_residual_noalloc", ctypes.c_int, [ctypes.c_int] * 3 + [ctypes.c_double] * 4 + [ctypes.c_int, _DP, _VP, _VP,
                                                                                       ctypes.c_int, _VP, _VP, _VP,
                                                                                       _VP, _VP]),
+    ("qms_residual_noalloc_fits", ctypes.c_int, [ctypes.c_int] * 3),
     ("qms_srv_create", ctypes.c_int, [ctypes.POINTER(QmsSrvDesc), ctypes.POINTER(_H)]),
     ("qms_srv_submit", ctypes.c_int, [_H, ctypes.POINTER(QmsRequest), ctypes.POINTER(ctypes.c_longlong)]),
     ("qms_srv_poll", ctypes.c_int, [_H, ctypes.c_longlong, ctypes.POINTER(QmsSrvResult)]),

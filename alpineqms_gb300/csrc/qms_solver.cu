@@ -1026,13 +1026,13 @@ int QmsSolver::inner_pcg(bool transient, int& iters) {
     return 0;
 }
 
-void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], bool exact) {
+int QmsSolver::residual_launch(bool adv, bool transient, const double v[3], bool exact) {
     if (start_resid_ready && !exact) {
         // the step start (qk_step_start) formed this residual and its partials
         start_resid_ready = false;
         last_resid_df = true;
         finalize(FIN_RESID, 4, nbop);
-        return;
+        return 0;
     } else if (df_resid && anchor_ready && anchor_is_residual && !exact) {
         // x is the anchor state: the residual is the anchor's
         OpEv* ev = prof_begin(3, (double)g.n * 8 * 3);
@@ -1058,13 +1058,14 @@ void QmsSolver::residual_launch(bool adv, bool transient, const double v[3], boo
             // the anchor of the double-float residuals that follow in this solve (an exact
             // residual asked for between solves leaves the anchor and its chain as they are)
             qms_launch_split_ref_pl(g, r64, r0df, rpl, st);
-            cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st);
+            CK(cudaMemcpyAsync(x0, x, g.n * 8, cudaMemcpyDeviceToDevice, st));
             nlaunch++;
             anchor_ready = true;
         }
         last_resid_df = false;
     }
     finalize(FIN_RESID, 4, nbop);
+    return 0;
 }
 
 template <typename T>
@@ -1090,7 +1091,8 @@ void QmsSolver::ensure_b() {
 }
 
 int QmsSolver::residual(bool adv, bool transient, const double v[3], bool exact) {
-    residual_launch(adv, transient, v, exact);
+    int rc = residual_launch(adv, transient, v, exact);
+    if (rc) return rc;
     CK(cudaGetLastError());
     return read_scalars();
 }
@@ -1137,7 +1139,7 @@ int QmsSolver::ir_iteration_graph(bool adv, bool transient, const double v[3], i
         if (e == cudaSuccess) {
             int it = 0;
             rc = fp64_inner ? inner_gmres<double>(adv, transient, v, it, k) : inner_gmres<float>(adv, transient, v, it, k);
-            residual_launch(adv, transient, v);
+            if (rc == 0) rc = residual_launch(adv, transient, v);
             G->resid_df = last_resid_df;
         }
         cudaGraph_t graph = nullptr;

@@ -157,7 +157,7 @@ struct QmsSolver {
     template <typename T> int inner_bicgstab(bool adv, bool transient, const double v[3], int& iters);
     template <typename T> int inner_pcg(bool transient, int& iters);
     template <typename T> int inner_gmres(bool adv, bool transient, const double v[3], int& iters, int fixed_k);
-    void residual_launch(bool adv, bool transient, const double v[3], bool exact = false);
+    int residual_launch(bool adv, bool transient, const double v[3], bool exact = false);
     int ir_iteration_graph(bool adv, bool transient, const double v[3], int k);
     // captured refinement iterations, one per FGMRES count k (and step parameters); the
     // profile event records of a capture belong to its entry

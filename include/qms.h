@@ -126,7 +126,7 @@ typedef struct {
 
 typedef struct qms_handle qms_handle;
 
-/* Fills `d` with the defaults for a grid (mixed precision, tol 1e-12). */
+/* Fills `d` with the defaults for a grid (mixed precision, tol 2e-13). */
 void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy, double dz, double dt);
 /* Device bytes a handle with this descriptor allocates (admission control). */
 size_t qms_device_bytes(const qms_desc* d);
@@ -205,9 +205,9 @@ void* qms_get_stream(qms_handle* h);
 /* Residual check for callers that cannot allocate device memory.  This entry
  * point has no counterpart in the reference (whose solve is a direct PARDISO
  * call with no residual output).  It is meant for code that may not call
- * cudaMalloc -- for example code running inside a CUDA stream capture of its
- * own, or a process whose device memory is owned by another runtime's pool --
- * and therefore cannot create a qms_handle.  It computes, on `stream`,
+ * cudaMalloc -- for example an allocator-free real-time loop, or a process
+ * whose device memory is owned by another runtime's pool -- and therefore
+ * cannot create a qms_handle.  It computes, on `stream`,
  *   d_r    = D^-1 (b - M x)                      (n_dims doubles, D = diag M)
  *   d_sums = |r_A|^2, |r_V|^2, |x_A|^2, |x_V|^2  (4 doubles)
  * for the steady (transient = 0) or transient operator with frame velocity v,
@@ -216,14 +216,21 @@ void* qms_get_stream(qms_handle* h);
  * doubles (mu_r x,y,z, sigma x,y,z).  It allocates nothing: its scratch is a
  * fixed static device array sized for at most 32768 operator tiles (grids up
  * to about 512 x 512 x 256 cells, or any grid with
- * ceil((xs+1)/32) * ceil((ys+1)/8) * ceil((zs+1)/16) <= 32768); larger grids are
- * rejected with QMS_ERR_ARG.  The first call on a device looks up the scratch
- * address on that device (make it before any stream capture).  All calls share
- * the scratch: calls that overlap on the GPU race, so serialise them (the call
- * returns after synchronising `stream`). */
+ * ceil((xs+1)/32) * ceil((ys+1)/8) * ceil((zs+1)/16) <= 32768; see
+ * qms_residual_noalloc_fits); larger grids are rejected with QMS_ERR_ARG
+ * before any launch.  The first call on a device looks up the scratch address
+ * on that device.  The call synchronises `stream` before it returns, so it
+ * must not be made while `stream` (or a stream it waits on) is being captured
+ * into a CUDA graph.  All calls on one device share the scratch: they are
+ * serialised on the host, and calls that overlap on the GPU (from other
+ * processes) race.  It returns QMS_ERR_CUDA without launching anything when
+ * the calling thread has an uncollected CUDA error. */
 int qms_residual_noalloc(int xs, int ys, int zs, double dx, double dy, double dz, double dt, int transient,
                          const double v[3], const uint8_t* d_slots, const double* rows, int nmat,
                          const double* d_x, const double* d_b, double* d_r, double* d_sums, void* stream);
+/* 1 when qms_residual_noalloc's fixed scratch holds a grid of xs x ys x zs cells, 0 otherwise
+ * (host arithmetic only; no CUDA call). */
+int qms_residual_noalloc_fits(int xs, int ys, int zs);
 
 /* ------------------------------------------------------------------------
  * Serving: whole solves (the content of one inputs.txt + geom.bin pair, as
@@ -300,6 +307,9 @@ int qms_srv_wait(qms_server* s, long long id, qms_srv_result* out);      /* unti
  * each the three components (Hx, Hy, Hz) of the slice back to back.  Copies at
  * most `cap` values; returns the number copied or a negative error. */
 long long qms_srv_slices(qms_server* s, long long id, double* out, long long cap);
+/* The error message of a failed or rejected request ("" otherwise; a fixed message for an
+ * unknown id).  A request's message is written once, when it ends, and requests are never
+ * removed from the server, so the pointer stays valid until qms_srv_destroy. */
 const char* qms_srv_error(qms_server* s, long long id);
 int qms_srv_stats_get(qms_server* s, qms_srv_stats* out);
 /* Waits for every queued and running request, then frees the server. */

@@ -1,7 +1,7 @@
 """Generate golden fixtures by executing the reference program itself.
 
 Run in a container where the reference checkout is mounted (the path is the
-first argument, default /root/reference).  For each case below this script:
+first argument, required).  For each case below this script:
 
 1. writes ``inputs.txt`` and ``geom.bin`` in a scratch directory, in the
    grammar of 3D/master.py:16-77;
@@ -19,7 +19,7 @@ The fixtures are small (grids of 6-9 cells per side).  They pin the CPU
 oracle (oracle/qms_oracle.c) and the host-side dump writer; the GPU tests
 then compare against the oracle.
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py /path/to/reference
 """
 from __future__ import annotations
 
@@ -143,7 +143,9 @@ def run_case(src, c, workdir):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/reference  (the AlpineQMS checkout)")
+    ref = sys.argv[1]
     src = os.path.join(ref, "3D", "QMS_3D.f90")
     for c in cases():
         with tempfile.TemporaryDirectory() as td:

@@ -111,3 +111,17 @@ def test_default_descriptor(lib):
     assert d.tol == 2e-13 and d.gmres_m == 32 and d.max_outer == 60
     assert d.mg_sweeps == 3 and d.mg_omega == 0.85 and d.mg_alpha == 1.5
     assert d.mg_coupling == 1 and d.extrapolate == 3
+
+
+def test_noalloc_size_query(lib):
+    """qms_residual_noalloc_fits (host arithmetic only) accepts grids whose operator tiles fit the
+    no-allocation entry point's fixed scratch (32768 tiles of 32 x 8 x 16 nodes) and rejects
+    larger ones; qms_residual_noalloc turns the same grids away before any launch."""
+    def tiles(xs, ys, zs):
+        return -(-(xs + 1) // 32) * -(-(ys + 1) // 8) * -(-(zs + 1) // 16)
+    for shape in [(4, 4, 4), (32, 32, 32), (256, 256, 256), (512, 512, 256), (2048, 2048, 2048), (3, 8, 8),
+                  (1000, 1000, 100)]:
+        want = 1 if min(shape) >= 4 and tiles(*shape) <= 32768 else 0
+        assert lib.qms_residual_noalloc_fits(*shape) == want, shape
+    assert lib.qms_residual_noalloc_fits(512, 512, 256) == 1
+    assert lib.qms_residual_noalloc_fits(2048, 2048, 2048) == 0

@@ -1,15 +1,16 @@
 """qms_residual_noalloc: the residual entry point for callers that cannot allocate.
 
-Callers such as code running inside someone else's CUDA stream capture, or
-a process whose device memory belongs to another runtime's pool, cannot
-call cudaMalloc and cannot create a qms_handle.  qms_residual_noalloc takes
+Callers such as an allocator-free real-time loop, or a process whose device
+memory belongs to another runtime's pool, cannot call cudaMalloc and cannot
+create a qms_handle.  qms_residual_noalloc takes
 only their own device buffers and keeps its scratch in fixed-size static
 device arrays.  This test calls it through the C-ABI twice in a row and checks
 each result against qms_residual_norm (the handle-based entry point) on the
 same state and right-hand side.
 
 The file is named so that pytest collects it last; it also passes alone in a
-fresh process.
+fresh process.  (The size limit of its fixed scratch is checked on the CPU
+through qms_residual_noalloc_fits in tests/test_capi_cpu.py.)
 """
 import ctypes
 
@@ -96,13 +97,3 @@ def test_noalloc_residual_matches_handle_entry_point():
         r = t_r.cpu().numpy()
         assert abs(np.sqrt(np.dot(r, r)) - np.sqrt(sums[0] + sums[1])) <= 1e-12 * np.sqrt(sums[0] + sums[1])
     s.close()
-
-
-def test_noalloc_rejects_oversize_grid():
-    if not torch.cuda.is_available():
-        pytest.skip("no CUDA device")
-    from alpineqms_gb300._lib import dvec
-    fn = _noalloc_fn()
-    # 2048^3 cells needs more operator CTAs than the fixed scratch holds: rejected before any launch
-    rc = fn(2048, 2048, 2048, 1e-3, 1e-3, 1e-3, 1e-5, 1, dvec([0, 0, 0]), 16, None, 0, 16, 16, 16, 16, None)
-    assert rc == -1
