@@ -99,6 +99,9 @@ QMS_KEEP_NONE, QMS_KEEP_SLICES = 0, 1
 QMS_EXC_NONE, QMS_EXC_COS, QMS_EXC_SIN = 0, 1, 2
 QMS_PREC_MIXED, QMS_PREC_FP64 = 0, 1
 QMS_FIELD_CUBES, QMS_FIELD_SLICE = 0, 1
+# qms_stats.status bits
+QMS_STATUS_BAD_MATERIAL, QMS_STATUS_NAN, QMS_STATUS_NO_CONVERGENCE = 1, 2, 4
+QMS_STATUS_BREAKDOWN, QMS_STATUS_TIMEOUT = 8, 16
 ERRORS = {-1: "QMS_ERR_ARG", -2: "QMS_ERR_CUDA", -3: "QMS_ERR_NOMEM", -4: "QMS_ERR_STATE", -5: "QMS_ERR_CONVERGE"}
 
 # (name, restype, argtypes) -- the full export table of include/qms.h
@@ -119,6 +122,7 @@ SIGNATURES = [
     ("qms_steady", ctypes.c_int, [_H, _DP, _DP, _DP]),
     ("qms_step", ctypes.c_int, [_H, _DP, _DP, _DP]),
     ("qms_get_stats", ctypes.c_int, [_H, ctypes.POINTER(QmsStats)]),
+    ("qms_wait_selftest", ctypes.c_int, [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_uint)]),
     ("qms_get_fields", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP]),
     ("qms_get_state", ctypes.c_int, [_H, _VP]),
     ("qms_get_rhs", ctypes.c_int, [_H, _VP]),

@@ -1,5 +1,6 @@
 // qms_capi.cu -- extern "C" entry points of libqms_gb300.so (declared in include/qms.h).
 #include "qms_solver.h"
+#include "qms_pl.h"
 
 #include <cmath>
 #include <cstring>
@@ -169,6 +170,24 @@ int qms_step(qms_handle* h, const double v[3], const double B[3], const double G
 int qms_get_stats(const qms_handle* h, qms_stats* out) {
     if (!h || !out) return QMS_ERR_ARG;
     *out = h->s.stats;
+    return 0;
+}
+
+int qms_wait_selftest(qms_handle* h, int spins, unsigned* status_out) {
+    HCHECK(h);
+    if (spins < 1 || spins > (1 << 20)) { h->s.err = "spins must be in 1..2^20"; return QMS_ERR_ARG; }
+    CKH(cudaSetDevice(h->s.dev));
+    cudaStream_t st = h->s.st;
+    CKH(cudaMemsetAsync(h->s.status, 0, sizeof(unsigned), st));
+    qms_launch_wait_selftest(spins, h->s.status, st);
+    CKH(cudaGetLastError());
+    unsigned stt = 0;
+    CKH(cudaMemcpyAsync(&stt, h->s.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CKH(cudaStreamSynchronize(st));
+    CKH(cudaMemsetAsync(h->s.status, 0, sizeof(unsigned), st));
+    h->s.stats = qms_stats{};
+    h->s.stats.status = stt;
+    if (status_out) *status_out = stt;
     return 0;
 }
 

@@ -19,6 +19,25 @@
 #include <mutex>
 
 // ---------------------------------------------------------------------------
+// Self-test of the bounded tile wait (mbar_wait_n, the wait every staged kernel uses): one CTA
+// waits on an mbarrier that nothing arrives at and no copy targets, gives up after `spins`
+// polls, flags QMS_ST_TIMEOUT and returns.  The context stays usable.
+// ---------------------------------------------------------------------------
+__global__ void qk_wait_selftest(int spins, unsigned* err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    mbar_wait_n(&bar, 0, err, spins);    // the barrier's first phase never completes
+}
+
+void qms_launch_wait_selftest(int spins, unsigned* err, cudaStream_t st) {
+    qk_wait_selftest<<<1, 32, 0, st>>>(spins, err);
+}
+
+// ---------------------------------------------------------------------------
 // tensor maps
 // ---------------------------------------------------------------------------
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {

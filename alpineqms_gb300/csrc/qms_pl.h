@@ -64,6 +64,9 @@ void qms_launch_split_ref_pl(const QGrid& g, const double* src, qdf* dst, float*
 void qms_launch_split_flat(long long n, const double* src, qdf* dst, cudaStream_t st);
 void qms_launch_pl_scale(long long n, const float* r, const double* scale, float* out, cudaStream_t st);
 
+// one CTA waiting (at most `spins` polls) on an mbarrier that never completes: sets QMS_ST_TIMEOUT
+void qms_launch_wait_selftest(int spins, unsigned* err, cudaStream_t st);
+
 void qms_launch_diag_pl(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st);
 
 // out[PL] = r64[ref] * scale[0] (scale may be null: 1)

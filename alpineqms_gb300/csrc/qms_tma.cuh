@@ -70,11 +70,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
 // for a hardware time limit per call, and after QMS_MBAR_SPINS calls the wait gives up,
 // flags QMS_ST_TIMEOUT in *err and returns false (the caller then stops using the tile).
 #define QMS_MBAR_SPINS (1 << 22)
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned* err) {
-    for (int it = 0; it < QMS_MBAR_SPINS; it++)
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, unsigned parity, unsigned* err, int spins) {
+    for (int it = 0; it < spins; it++)
         if (mbar_try_wait(bar, parity)) return true;
     if (err) atomicOr(err, (unsigned)QMS_ST_TIMEOUT);
     return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned* err) {
+    return mbar_wait_n(bar, parity, err, QMS_MBAR_SPINS);
 }
 
 // one 4-D tiled bulk tensor copy global -> shared, completion counted on `bar`

@@ -149,6 +149,13 @@ int qms_set_geometry_f64(qms_handle* h, const double* geom, const double* table,
 int qms_steady(qms_handle* h, const double v[3], const double B[3], const double G[9]);
 int qms_step(qms_handle* h, const double v[3], const double B[3], const double G[9]);
 int qms_get_stats(const qms_handle* h, qms_stats* out);
+/* Failure-detection self-test (no counterpart in the reference, whose PARDISO error code is
+ * never checked, F:2196-2202): one CTA on the handle's stream waits on a shared-memory
+ * mbarrier that nothing completes, with the bounded wait every TMA-staged kernel uses for its
+ * tile copies (here at most `spins` polls, 1..2^20).  The wait gives up, the kernel returns
+ * and sets QMS_STATUS_TIMEOUT, which is reported in *status_out (may be NULL) and in
+ * qms_get_stats; the handle stays usable for the next call. */
+int qms_wait_selftest(qms_handle* h, int spins, unsigned* status_out);
 
 /* which = QMS_FIELD_CUBES: out = Hx|Hy|Hz cubes (3*xs*ys*zs doubles, F-order);
  * which = QMS_FIELD_SLICE: out = the three slices (axis 0/1/2 = x/y/z, 1-based
