@@ -41,7 +41,8 @@ class QmsDesc(ctypes.Structure):
                 ("use_graphs", ctypes.c_int), ("mg_region_cut", ctypes.c_double),
                 ("mg_alpha", ctypes.c_double), ("mg_coupling", ctypes.c_int),
                 ("mg_coarse_sweeps", ctypes.c_int), ("mg_v_sweeps", ctypes.c_int),
-                ("mg_tail_points", ctypes.c_int), ("extrapolate", ctypes.c_int)]
+                ("mg_tail_points", ctypes.c_int), ("extrapolate", ctypes.c_int),
+                ("mg_v_coarse_cut", ctypes.c_double)]
 
 
 class QmsStats(ctypes.Structure):

@@ -872,7 +872,7 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
             // V block: pseudo-inverse.  An isolated conductor's potential is pinned only by the
             // 1e-12 S/m floor; on the coarsest grid that is an eigenvalue ~1e-19 of the
             // diagonally scaled operator.  Inverting it would amplify round-off without bound,
-            // so eigenvalues below 1e-9 are dropped (the mode does not enter A or H).
+            // so eigenvalues at or below `vcut` are dropped (the mode does not enter A or H).
             std::vector<double> dsq(m);
             for (int r = 0; r < m; r++) dsq[r] = 1.0 / std::sqrt(std::fabs(A[(size_t)r * m + r]));
             for (int r = 0; r < m; r++)
@@ -889,7 +889,7 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
                     double acc = 0.0;
                     for (int e = 0; e < m; e++) {
                         const double lam = A[(size_t)e * m + e];
-                        if (lam > 1e-9) acc += Q[(size_t)r * m + e] * Q[(size_t)q * m + e] / lam;
+                        if (lam > vcut) acc += Q[(size_t)r * m + e] * Q[(size_t)q * m + e] / lam;
                     }
                     Inv[(size_t)r * m + q] = dsq[r] * acc * dsq[q];
                 }

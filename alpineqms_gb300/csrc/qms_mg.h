@@ -52,6 +52,7 @@ struct QmsMG {
     QCoef<T> c0{};
     QStepPar<T> P0{};
     T vshift0 = T(0);
+    double vcut = 1e-9;            // coarsest V level: eigenvalues (diagonally scaled) at or below this are dropped
     dim3 g0grid, g0block;
     std::string err;
 

@@ -114,6 +114,9 @@ typedef struct {
                                 3 (default) cubic, 4 x_n - 6 x_(n-1) + 4 x_(n-2) - x_(n-3);
                                 2 quadratic, 3 x_n - 3 x_(n-1) + x_(n-2); 1 linear,
                                 2 x_n - x_(n-1); 0 none */
+    double mg_v_coarse_cut;  /* coarsest multigrid level of the potential block: eigenvalues of its
+                                diagonally scaled operator at or below this are dropped from its
+                                pseudo-inverse (0 = automatic: 1e-9) */
 } qms_desc;
 
 typedef struct {
