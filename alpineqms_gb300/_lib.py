@@ -58,7 +58,8 @@ class QmsProfile(ctypes.Structure):
                 ("op32_launches", ctypes.c_int64), ("op32_ms", ctypes.c_double), ("op32_bytes", ctypes.c_double),
                 ("op64_launches", ctypes.c_int64), ("op64_ms", ctypes.c_double), ("op64_bytes", ctypes.c_double),
                 ("mg_cycles", ctypes.c_int64), ("mg_ms", ctypes.c_double),
-                ("resid_launches", ctypes.c_int64), ("resid_ms", ctypes.c_double), ("resid_bytes", ctypes.c_double)]
+                ("resid_launches", ctypes.c_int64), ("resid_ms", ctypes.c_double), ("resid_bytes", ctypes.c_double),
+                ("mg0a_launches", ctypes.c_int64), ("mg0a_ms", ctypes.c_double), ("mg0a_bytes", ctypes.c_double)]
 
 
 class QmsSrvDesc(ctypes.Structure):

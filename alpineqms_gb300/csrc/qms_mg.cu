@@ -996,8 +996,16 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
         MG0(0, x, x.p, nullptr);
         launches++;
     }
+    // the A-block sweeps are the largest single kernel of a transient step: optionally timed,
+    // with their algorithmic bytes (x and b read, x written, one material byte per cell)
+    const double asweep_bytes = 3.0 * sizeof(T) * (double)g0.oV + (double)g0.xs * g0.ys * g0.zs;
+    auto sweep = [&](Buf& xi, T* xo) {
+        void* tok = (QS == 1 && prof) ? prof->begin(MGPROF_A_SWEEP, asweep_bytes) : nullptr;
+        MG0(1, xi, xo, nullptr);
+        if (tok) prof->end(tok);
+    };
     for (; s < n1; s++) {
-        MG0(1, x, t.p, nullptr);
+        sweep(x, t.p);
         std::swap(x, t);
         launches++;
     }
@@ -1062,7 +1070,7 @@ int QmsMG<T>::vcycle_q(const T* b0, bool scaled, T* x0, const CUtensorMap& x0map
     mg0_prolong<T, QS><<<qms_node_grid(g0), qms_node_block(), 0, st>>>(g0, mv, x.p, lv[1], lv[1].x, alpha);
     launches++;
     for (int s = 0; s < n2; s++) {
-        MG0(1, x, t.p, nullptr);
+        sweep(x, t.p);
         std::swap(x, t);
         launches++;
     }

@@ -30,6 +30,15 @@ struct MGLevelDev {
     T* t;                   // Jacobi temporary
 };
 
+// Optional timing of selected multigrid launches (CUDA events bracketing them on the stream):
+// begin() returns a token for end(), or null when profiling is off.
+struct MgProf {
+    virtual void* begin(int kind, double bytes) = 0;
+    virtual void end(void* token) = 0;
+    virtual ~MgProf() {}
+};
+enum { MGPROF_A_SWEEP = 4 };     // a level-0 Jacobi sweep on the three A blocks (mg0_tiled, KIND 1, QS 1)
+
 template <typename T>
 struct QmsMG {
     std::vector<MGLevelDev<T>> lv;
@@ -52,6 +61,7 @@ struct QmsMG {
     QCoef<T> c0{};
     QStepPar<T> P0{};
     T vshift0 = T(0);
+    MgProf* prof = nullptr;
     double vcut = 1e-9;            // coarsest V level: eigenvalues (diagonally scaled) at or below this are dropped
     dim3 g0grid, g0block;
     std::string err;

@@ -528,6 +528,8 @@ void QmsSolver::release() {
 
 int QmsSolver::init(const qms_desc& d) {
     desc = d;
+    mghook.s = this;
+    for (int q = 0; q < 2; q++) { mgf[q].prof = &mghook; mgd[q].prof = &mghook; }
     dev = d.device;
     CK(cudaSetDevice(dev));
     if (d.xs < 4 || d.ys < 4 || d.zs < 4) { err = "grid must have at least 4 cells per axis"; return QMS_ERR_ARG; }
@@ -814,6 +816,7 @@ bool QmsSolver::prof_accum(const OpEv& e) {
     if (e.kind == 1) { profacc.op64_launches++; profacc.op64_ms += ms; profacc.op64_bytes += e.bytes; }
     else if (e.kind == 0) { profacc.op32_launches++; profacc.op32_ms += ms; profacc.op32_bytes += e.bytes; }
     else if (e.kind == 3) { profacc.resid_launches++; profacc.resid_ms += ms; profacc.resid_bytes += e.bytes; }
+    else if (e.kind == MGPROF_A_SWEEP) { profacc.mg0a_launches++; profacc.mg0a_ms += ms; profacc.mg0a_bytes += e.bytes; }
     else { profacc.mg_cycles++; profacc.mg_ms += ms; }
     return true;
 }

@@ -115,7 +115,8 @@ struct QmsSolver {
     // instrumentation (qms_profile_enable)
     bool prof = false;
     long long nlaunch = 0;
-    struct OpEv { cudaEvent_t a, b; int kind; double bytes; };   // kind: 0 op32, 1 op64, 2 V-cycle, 3 FP64 residual
+    // kind: 0 op32, 1 op64, 2 V-cycle, 3 FP64 residual, 4 level-0 A-block Jacobi sweep
+    struct OpEv { cudaEvent_t a, b; int kind; double bytes; };
     OpEv* prof_begin(int kind, double bytes);
     void prof_end(OpEv* ev);
     bool prof_accum(const OpEv& e);              // false when the events cannot be timed
@@ -124,6 +125,12 @@ struct QmsSolver {
     bool capturing = false;                      // event records go into a graph being captured
     bool graph_prof_broken = false;
     qms_profile profacc{};
+    // the multigrid's timing hook (the A-block sweeps), forwarding to prof_begin / prof_end
+    struct MgHook : MgProf {
+        QmsSolver* s = nullptr;
+        void* begin(int kind, double bytes) override { return s->prof_begin(kind, bytes); }
+        void end(void* token) override { s->prof_end((OpEv*)token); }
+    } mghook;
     int profile_enable(bool on);
     int profile_collect(qms_profile* out);
     template <typename T>

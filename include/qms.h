@@ -206,6 +206,9 @@ typedef struct {
     int64_t resid_launches;  /* FP64 refinement residuals r = D^-1 (b - M x) */
     double resid_ms;
     double resid_bytes;
+    int64_t mg0a_launches;   /* level-0 Jacobi sweeps on the three A blocks (the largest kernel of a step) */
+    double mg0a_ms;
+    double mg0a_bytes;       /* their algorithmic bytes: x and b read, x written (3 p n_A), one byte per cell */
 } qms_profile;
 int qms_profile_enable(qms_handle* h, int on);
 int qms_get_profile(qms_handle* h, qms_profile* out);
