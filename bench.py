@@ -55,7 +55,9 @@ def parse_args():
     ap.add_argument("--cpu-steps", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 step comparison")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the plain FP64 GPU solver leg (its timing and the per-step comparison)")
+    ap.add_argument("--workload", default="moving_plate_256", choices=WORKLOADS)
     ap.add_argument("--check-every", type=int, default=None)
     ap.add_argument("--set", action="append", default=[], metavar="FIELD=VALUE",
                     help="override a qms_desc field of the timed solver (e.g. gmres_m=24, mg_alpha=1.8)")
@@ -202,56 +204,72 @@ def aggregate_replicas(ms_local, units_local, dist=None, device="cpu"):
     return float(mx.item()), float(sm.item())
 
 
-def edge_current(inp, geom, x):
-    """sigma_edge * dV/dh on every x-, y- and z-edge (sigma_edge the mean of the four cells
-    around the edge): how V enters the A rows.  Used to compare potentials up to the
-    floating constant of isolated conductors."""
-    import numpy as np
-    xs, ys, zs = inp.xs, inp.ys, inp.zs
-    Nx, Ny, Nz = xs + 1, ys + 1, zs + 1
-    oV = 4 * Nx * Ny * Nz - Ny * Nz - Nx * Nz - Nx * Ny - Nx * Ny * Nz
-    V = np.asarray(x[oV:]).reshape((Nx, Ny, Nz), order="F")
-    g = np.asarray(geom).reshape((xs, ys, zs), order="F")
-    table = inp.props_table()
-    lut = {int(r[0]): r[4:7] for r in table}
-    sig = np.zeros((3, xs, ys, zs))
-    for mid, sv in lut.items():
-        m = g == mid
-        for a in range(3):
-            sig[a][m] = sv[a]
-    out = []
-    for a, (d, n) in enumerate(((inp.dx, xs), (inp.dy, ys), (inp.dz, zs))):
-        s = np.pad(sig[a], 1)                   # cells with a zero halo
-        # edge along axis a from node p: the four cells sharing it (other two indices p-1, p)
-        if a == 0:
-            se = 0.25 * (s[1:-1, :-1, :-1] + s[1:-1, 1:, :-1] + s[1:-1, :-1, 1:] + s[1:-1, 1:, 1:])
-            dv = (V[1:] - V[:-1]) / d
-        elif a == 1:
-            se = 0.25 * (s[:-1, 1:-1, :-1] + s[1:, 1:-1, :-1] + s[:-1, 1:-1, 1:] + s[1:, 1:-1, 1:])
-            dv = (V[:, 1:] - V[:, :-1]) / d
-        else:
-            se = 0.25 * (s[:-1, :-1, 1:-1] + s[1:, :-1, 1:-1] + s[:-1, 1:, 1:-1] + s[1:, 1:, 1:-1])
-            dv = (V[:, :, 1:] - V[:, :, :-1]) / d
-        # the reference forms edge conductivities only for node indices 2..size (F:258-269)
-        mask = np.zeros(se.shape, bool)
-        mask[1:xs if a != 0 else xs, 1:ys if a != 1 else ys, 1:zs if a != 2 else zs] = True
-        if a == 0:
-            mask[0] = False
-        elif a == 1:
-            mask[:, 0] = False
-        else:
-            mask[:, :, 0] = False
-        out.append((np.where(mask, se, 0.0) * dv).ravel(order="F"))
-    return np.concatenate(out)
+WORKLOADS = ("moving_plate_256", "inclusions_96", "laminated_core", "plain_block_32")
 
 
-# ---------------------------------------------------------------------------
+def make_workload(args, nt):
+    from alpineqms_gb300 import workloads
+    if args.workload == "moving_plate_256":
+        return workloads.moving_plate(args.size, nt=nt)
+    if args.workload == "inclusions_96":
+        return workloads.inclusions_96(nt=nt)
+    if args.workload == "laminated_core":
+        return workloads.laminated_core(nt=nt)
+    return workloads.plain_block_32(nt=nt)
+
+
+class Run:
+    """One solver handle driven through a workload's steps: steady init, then transient steps
+    with the velocity of trajectory type 1 and the (possibly AC) background field of each step."""
+
+    def __init__(self, inp, geom, desc):
+        from alpineqms_gb300.solver import QMSSolver
+        from alpineqms_gb300.trajectory import VelocitySchedule
+        self.inp = inp
+        self.s = QMSSolver(desc)
+        self.s.set_geometry_f64(geom, inp.props_table())
+        self.sched = VelocitySchedule(inp.traj, inp.dt)
+        self.counter = 0
+
+    def field(self, k):
+        from alpineqms_gb300.trajectory import scaled_field
+        return scaled_field(self.inp.B, self.inp.G, self.inp.excitation, k * self.inp.dt)
+
+    def steady(self):
+        B, G = self.field(0)
+        return self.s.steady(self.sched.steady(), B, G)
+
+    def args_of_next(self):
+        k = self.counter + 1
+        B, G = self.field(k)
+        return self.sched.step(k), B, G
+
+    def step(self):
+        v, B, G = self.args_of_next()
+        self.counter += 1
+        return self.s.step(v, B, G)
+
+    def close(self):
+        self.s.close()
+
+
+def timed_steps(run, k, ext):
+    """k steps bracketed by CUDA events on the library's stream (inputs resident)."""
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(ext)
+    its = [run.step() for _ in range(k)]
+    ev1.record(ext)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1), its
+
+
 def run_gpu(args):
     import numpy as np
     import torch
-    from alpineqms_gb300 import workloads
-    from alpineqms_gb300.solver import QMSSolver, default_desc
-    from alpineqms_gb300.trajectory import VelocitySchedule, scaled_field
+    from alpineqms_gb300 import compare
+    from alpineqms_gb300.solver import default_desc
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -262,166 +280,165 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    inp, geom = workloads.moving_plate(args.size, nt=args.steps + args.warmup + 1)
+    W, K = args.warmup, args.steps
+    inp, geom = make_workload(args, W + 2 * K + 4)
     kw = {}
     if args.check_every:
         kw["check_every"] = args.check_every
     for item in args.set:
         key, _, val = item.partition("=")
         kw[key] = float(val) if any(ch in val for ch in ".eE") else int(val)
-    desc = default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt, precision=args.precision,
-                        device=local, **kw)
-    solver = QMSSolver(desc)
-    solver.set_geometry_f64(geom, inp.props_table())
-    n = solver.n
-    sched = VelocitySchedule(inp.traj, inp.dt)
-    B, G = scaled_field(inp.B, inp.G, inp.excitation, 0.0)
-    t0 = time.perf_counter()
-    st0 = solver.steady(sched.steady(), B, G)
-    steady_s = time.perf_counter() - t0
-    counter = 0
-    for _ in range(args.warmup):
-        counter += 1
-        solver.step(sched.step(counter), B, G)
 
-    ext = torch.cuda.ExternalStream(solver.stream_ptr())
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    def desc_of(precision, **extra):
+        return default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt, precision=precision,
+                            device=local, **{**kw, **extra})
+
+    desc = desc_of(args.precision)
+
+    # -- 1. device-timed pass: W untimed steps, then K steps between CUDA events
+    run = Run(inp, geom, desc)
+    n = run.s.n
+    t0 = time.perf_counter()
+    st0 = run.steady()
+    steady_s = time.perf_counter() - t0
+    for _ in range(W):
+        run.step()
+    ext = torch.cuda.ExternalStream(run.s.stream_ptr())
     clocks = ClockSampler(local)
-    iters = []
     if dist:
         dist.barrier()
-    torch.cuda.synchronize()
     clocks.start()
-    ev0.record(ext)
-    for _ in range(args.steps):
-        counter += 1
-        iters.append(solver.step(sched.step(counter), B, G))
-    ev1.record(ext)
-    torch.cuda.synchronize()
+    ms_local, iters = timed_steps(run, K, ext)
     clk = clocks.stop()
-    ms, units = aggregate_replicas(ev0.elapsed_time(ev1), n * args.steps, dist, "cuda")
+    ms, units = aggregate_replicas(ms_local, n * K, dist, "cuda")
     if dist:
         dist.barrier()
     value = units / (ms / 1e3)
+    run.close()
 
-    # Kernel timings: as many steps again with the profile on (CUDA events around every operator
-    # and V-cycle launch, recorded into the replayed graphs; two untimed steps first capture the
-    # graphs that carry them).  The event records cost time of their own, so this pass is timed
-    # apart from the one above and its step time is reported beside it.
-    solver.profile_enable(True)
-    for _ in range(2):
-        counter += 1
-        solver.step(sched.step(counter), B, G)
-    torch.cuda.synchronize()
-    solver.profile_enable(True)          # counts from here
-    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev2.record(ext)
-    piters = []
-    for _ in range(args.steps):
-        counter += 1
-        piters.append(solver.step(sched.step(counter), B, G))
-    ev3.record(ext)
-    torch.cuda.synchronize()
-    prof = solver.profile()
-    solver.profile_enable(False)
-    prof_ms_per_step = ev2.elapsed_time(ev3) / args.steps
-
-    # end to end through the public API: per step the velocity / field scalars come from
-    # pinned host memory and the H slice (what the reference dumps every step) is read back
+    # -- 2. end to end through the public API, on the same steps in the same solver states: a
+    # fresh handle replays the steady init and the W warm-up steps, then per step the velocity
+    # and field scalars come from pinned host memory and the H slice (what the reference dumps
+    # every step) is read back
     e2e = None
+    run = Run(inp, geom, desc)
+    run.steady()
+    for _ in range(W):
+        run.step()
     if not args.no_e2e:
         hostbuf = torch.empty(15, dtype=torch.float64).pin_memory()
         slice_bytes = 3 * inp.slice_shape()[0] * inp.slice_shape()[1] * 8
-        # two untimed steps capture the graphs without the profile's event records
-        for _ in range(2):
-            counter += 1
-            solver.step(sched.step(counter), B, G)
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        for _ in range(args.steps):
-            counter += 1
-            v = sched.step(counter)
+        for _ in range(K):
+            v, B, G = run.args_of_next()
             hostbuf[:3] = torch.tensor(v, dtype=torch.float64)
-            hostbuf[3:6] = torch.from_numpy(np.asarray(B))
-            hostbuf[6:15] = torch.from_numpy(np.asarray(G))
+            hostbuf[3:6] = torch.from_numpy(np.asarray(B, np.float64))
+            hostbuf[6:15] = torch.from_numpy(np.asarray(G, np.float64).reshape(9))
             hv = hostbuf.numpy()
-            solver.step(hv[:3], hv[3:6], hv[6:15])
-            solver.slices(inp.slice_axis, inp.slice_index)
+            run.s.step(hv[:3], hv[3:6], hv[6:15])
+            run.counter += 1
+            run.s.slices(inp.slice_axis, inp.slice_index)
         torch.cuda.synchronize()
-        e2e_ms, e2e_units = aggregate_replicas(1e3 * (time.perf_counter() - t1), n * args.steps, dist, "cuda")
+        e2e_ms, e2e_units = aggregate_replicas(1e3 * (time.perf_counter() - t1), n * K, dist, "cuda")
         e2e = {"value": e2e_units / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 15 * 8,
-               "d2h_bytes_per_step": slice_bytes}
+               "d2h_bytes_per_step": slice_bytes,
+               "steps": "the same steps (%d..%d) as the device-timed pass, from the same states" % (W + 1, W + K)}
+    else:
+        for _ in range(K):
+            run.step()
 
-    # Accuracy at the bench workload: one more step in both precisions from the same state,
-    # compared per unknown block (A, V) and on H, the field the reference dumps.
-    accuracy = None
-    if not args.no_accuracy and rank == 0 and args.precision == "mixed":
-        x_prev = solver.get_state()
-        counter += 1
-        v = sched.step(counter)
-        stm = solver.step(v, B, G)
-        xm = solver.get_state()
-        hm = [h.copy() for h in solver.fields()]
-        # the solver's own final residual (double-float, or from the Arnoldi relation) against
-        # the exact FP64 residual of the same state
-        r_exact = solver.residual_norm(True, v)
-        # the FP64 reference step is solved well below the mixed solver's tolerance, so the
-        # difference measures the mixed solver's error rather than the reference's
-        s64 = QMSSolver(default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt, precision="fp64",
-                                     device=local, tol=1e-14, max_outer=60))
-        s64.set_geometry_f64(geom, inp.props_table())
-        s64.set_state(x_prev)
-        st64 = s64.step(v, B, G)
-        xd = s64.get_state()
-        hd = s64.fields()
-        oV = n - (inp.xs + 1) * (inp.ys + 1) * (inp.zs + 1)
+    # -- 3. kernel timings: K more steps with the profile on (CUDA events around every operator,
+    # V-cycle and level-0 A-block sweep, recorded into the replayed graphs; two untimed steps
+    # first capture the graphs that carry them).  The event records cost time of their own, so
+    # this pass is timed apart from the one above and its step time is reported beside it.
+    run.s.profile_enable(True)
+    for _ in range(2):
+        run.step()
+    torch.cuda.synchronize()
+    run.s.profile_enable(True)          # counts from here
+    ext = torch.cuda.ExternalStream(run.s.stream_ptr())
+    prof_ms, _ = timed_steps(run, K, ext)
+    prof = run.s.profile()
+    run.s.profile_enable(False)
+    prof_ms_per_step = prof_ms / K
+    run.close()
 
-        def rel(a, b):
-            nb = float(np.linalg.norm(b))
-            return float(np.linalg.norm(a - b)) / nb if nb > 0 else float(np.linalg.norm(a))
-        jm, jd = edge_current(inp, geom, xm), edge_current(inp, geom, xd)
-        accuracy = {"vs": "fp64 GPU solver (tol 1e-14), same start state, one step", "step": counter,
-                    "rel_l2_A": rel(xm[:oV], xd[:oV]), "rel_l2_J": rel(jm, jd),
-                    "rel_l2_H": rel(np.concatenate([h.ravel() for h in hm]), np.concatenate([h.ravel() for h in hd])),
-                    "rel_l2_V_raw": rel(xm[oV:], xd[oV:]),
-                    "note": "V enters through sigma grad V (J); an isolated conductor's potential carries an "
-                            "arbitrary constant that no residual sees",
-                    "fp64_iters": {"outer": st64["outer"], "inner": st64["inner"]},
-                    "final_residual": {"reported": stm["r"], "fp64": r_exact, "tol": desc.tol}}
-        accuracy["pass_1e-8"] = all(accuracy[k] <= 1e-8 for k in ("rel_l2_A", "rel_l2_J", "rel_l2_H"))
-        s64.close()
+    # -- 4. the plain FP64 GPU solver (the same algorithm with every inner component in FP64, the
+    # same tolerance) over the same steps, in lockstep with a fresh mixed-precision run: its K
+    # steps after the same W warm-up are timed between CUDA events on its own stream, and after
+    # every step (outside the timed events) the two solutions are compared block by block
+    fp64 = accuracy = None
+    if rank == 0 and not args.no_fp64 and args.precision == "mixed":
+        esig = compare.edge_sigma(inp, geom)
+        fixer = compare.GaugeFixer(inp, geom, esig)
+        rm = Run(inp, geom, desc)
+        r64 = Run(inp, geom, desc_of("fp64"))
+        ext64 = torch.cuda.ExternalStream(r64.s.stream_ptr())
+        rm.steady()
+        r64.steady()
+        per_step = []
+        t64 = 0.0
+        it64 = []
+        for k in range(1, W + K + 1):
+            rm.step()
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(ext64)
+            s64 = r64.step()
+            ev1.record(ext64)
+            torch.cuda.synchronize()
+            if k > W:
+                t64 += ev0.elapsed_time(ev1)
+                it64.append({"outer": s64["outer"], "inner": s64["inner"]})
+            xm, xd = rm.s.get_state(), r64.s.get_state()
+            cmp = compare.compare_states(inp, geom, xm, xd, rm.s.fields(), r64.s.fields(), fixer, esig)
+            cmp["step"] = k
+            per_step.append(cmp)
+        rm.close()
+        r64.close()
+        fp64 = {"value": n * K / (t64 / 1e3), "unit": UNIT, "ms_per_step": t64 / K, "steps": K,
+                "tol": desc.tol, "iters": it64,
+                "mixed_over_fp64": value / (n * K / (t64 / 1e3))}
+        keys = ("A", "V_gauge_fixed", "J", "H")
+        worst = {q: max(r[q] for r in per_step) for q in keys}
+        accuracy = {"vs": "plain FP64 GPU solver at the same tolerance, same inputs, every step from the steady "
+                          "state (mixed and FP64 trajectories run independently)",
+                    "max_rel_l2": worst, "max_rel_l2_V_raw": max(r["V_raw"] for r in per_step),
+                    "pass_1e-8": all(worst[q] <= 1e-8 for q in ("A", "V_gauge_fixed", "H")),
+                    "V_gauge": "V on the nodes with a conducting edge, each floating body's mean removed (%d "
+                               "nodes, %d floating bodies)" % (fixer.nodes.size, int(fixer.floating.sum())),
+                    "H": "B / mu at the cell centres (the dumped field)",
+                    "per_step": per_step}
 
     peak, peak_kind = measured_peak()
-    # The roofline kernel is the inner solver's stencil (the TMA-staged operator on the padded
-    # layout): algorithmic bytes 2 p n + cells per launch (x and y, one material byte per cell).
-    inner = "fp32" if args.precision == "mixed" else "fp64"
-    kms = prof["op32_ms"] if inner == "fp32" else prof["op64_ms"]
-    kbytes = prof["op32_bytes"] if inner == "fp32" else prof["op64_bytes"]
-    klaunch = prof["op32_launches"] if inner == "fp32" else prof["op64_launches"]
-    kern = "qk_op_pl<float> (inner stencil, TMA)" if inner == "fp32" else "qk_op_pl<double> (inner stencil, TMA)"
+    # The roofline kernel is the largest single kernel of a step: the level-0 Jacobi sweep on
+    # the three A blocks (mg0_tiled<T, 1, 1>).  Algorithmic bytes per launch: x and b read, x
+    # written (3 p n_A) and one material byte per cell.
+    kms, kbytes, klaunch = prof["mg0a_ms"], prof["mg0a_bytes"], prof["mg0a_launches"]
     achieved = kbytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
-    tr = ncu_traffic("qk_op_pl_f32" if inner == "fp32" else "qk_op_pl_f64")
-    roofline = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+    p = 4 if args.precision == "mixed" else 8
+    tr = ncu_traffic("mg0_tiled_f32_a" if p == 4 else "mg0_tiled_f64_a")
+    n_a = n - (inp.xs + 1) * (inp.ys + 1) * (inp.zs + 1)
+    roofline = {"bound": "hbm", "kernel": "mg0_tiled<%s,1,1> (level-0 Jacobi sweep, A blocks, TMA)" %
+                                          ("float" if p == 4 else "double"),
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6800 GB/s",
-                "traffic": (tr * n if tr else None), "launches": klaunch,
+                "traffic": (tr * n_a if tr else None), "launches": klaunch,
                 "avg_launch_us": 1e3 * kms / max(klaunch, 1),
                 "algorithmic_bytes_per_launch": kbytes / max(klaunch, 1),
-                "algorithmic_bytes_def": "2 p n_dims + cells (x, y, one material byte per cell)",
-                "share_of_step": kms / (prof_ms_per_step * args.steps) if prof_ms_per_step > 0 else None,
-                "timed_pass": "the kernel timings come from a second pass of as many steps with CUDA events "
-                              "around every operator / V-cycle launch (%.2f ms per step there)" % prof_ms_per_step,
-                "op32_ms": prof["op32_ms"], "op64_ms": prof["op64_ms"], "mg_ms": prof["mg_ms"],
-                "mg_cycles": prof["mg_cycles"]}
-    if prof["resid_launches"] > 0:
-        # the refinement residuals: the FP64 anchor (bound by GB300's FP64 rate), the double-float
-        # ones from the anchor, and the chained step start
-        roofline["refinement_residual"] = {"launches": prof["resid_launches"], "ms": prof["resid_ms"],
-                                     "avg_launch_us": 1e3 * prof["resid_ms"] / prof["resid_launches"],
-                                     "achieved_gbs": prof["resid_bytes"] / (prof["resid_ms"] / 1e3) / 1e9
-                                     if prof["resid_ms"] > 0 else None}
+                "algorithmic_bytes_def": "3 p n_A + cells (x and b read, x written; one material byte per cell)",
+                "share_of_step": kms / (prof_ms_per_step * K) if prof_ms_per_step > 0 else None,
+                "timed_pass": "kernel timings from a later pass of as many steps with CUDA events around the "
+                              "timed launches (%.2f ms per step there)" % prof_ms_per_step,
+                "other_kernels_ms": {"op32": prof["op32_ms"], "op64": prof["op64_ms"], "vcycles": prof["mg_ms"],
+                                     "refinement_residual": prof["resid_ms"]}}
+    if prof["op32_launches"] > 0:
+        roofline["inner_stencil_fp32"] = {"launches": prof["op32_launches"],
+                                          "achieved_gbs": prof["op32_bytes"] / (prof["op32_ms"] / 1e3) / 1e9}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -431,11 +448,13 @@ def run_gpu(args):
             cpu = {"error": repr(e)}
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+                "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-                "config": {"workload": "moving_plate_256", "grid": [inp.xs, inp.ys, inp.zs], "dof": n,
+                "config": {"workload": args.workload if args.workload != "moving_plate_256" or args.size == 256
+                           else "moving_plate_%d" % args.size,
+                           "grid": [inp.xs, inp.ys, inp.zs], "dof": n,
                            "dt": inp.dt, "precision": args.precision, "tol": desc.tol,
                            "solver": {"krylov": "fgmres" if desc.krylov == 0 else "bicgstab",
                                       "gmres_m": desc.gmres_m, "mg_sweeps": desc.mg_sweeps,
@@ -447,13 +466,12 @@ def run_gpu(args):
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                            "l2": "inputs larger than L2 (one FP32 vector = %.0f MB)" % (n * 4 / 1e6)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": prof["launches"],
-                "accuracy": accuracy,
+                "fp64": fp64, "accuracy": accuracy,
                 "clocks": clk, "steady_s": steady_s,
                 "steady_iters": {"outer": st0["outer"], "inner": st0["inner"]},
-                "step_iters": [{"outer": s["outer"], "inner": s["inner"], "r0": s["r0"], "r": s["r"]}
-                               for s in iters]}
+                "step_iters": [{"outer": q["outer"], "inner": q["inner"], "r0": q["r0"], "r": q["r"]}
+                               for q in iters]}
         print(json.dumps(line))
-    solver.close()
     if dist:
         dist.destroy_process_group()
     return 0
