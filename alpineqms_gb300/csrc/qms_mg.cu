@@ -107,25 +107,32 @@ __device__ __forceinline__ bool mg_fine_active(const QGrid& g, int b, int i, int
 // coarse point (I,J,K) aggregates fine points (2I..2I+1, 2J..2J+1, 2K..2K+1) (0-based):
 // a coarse link is the sum of the fine links crossing between two aggregates, a
 // coarse diagonal the sum of the fine diagonals minus twice the internal links.
-// `fine(b, f, i, j, k, w1, w2, w3, d)` gives fine point f = (i, j, k) of block b and
-// returns whether it is active; `act(b, f, i, j, k)` only its activity.
+// `fine(b, f, i, j, k, w1, w2, w3, d, m)` gives fine point f = (i, j, k) of block b (m: the
+// summed level-0 diagonals it stands for) and returns whether it is active; `act(b, f, i, j, k)`
+// only its activity.
+// A coarse V point whose diagonal is at or below ncut times its summed level-0 diagonals is a
+// near-null mode (a floating conductor collapsed into one aggregate: the constant over it costs
+// almost no energy, and the computed diagonal is the cancellation noise of the sums above); it
+// leaves the hierarchy (inactive) instead of amplifying its right-hand side by 1 / noise.  The
+// conductor-region coarse space carries such modes exactly.
 template <typename T, typename Fine, typename Act>
 __device__ __forceinline__ void mg_coarsen_point(const MGBlockDesc& fb, const MGBlockDesc& cb, int b, long long t,
-                                                 MGLevelDev<T>& C, Fine fine, Act act) {
+                                                 MGLevelDev<T>& C, double ncut, Fine fine, Act act) {
     long long q = t - cb.off;
     int I, J, K;
     mg_ijk(q, cb.n1, cb.n2, I, J, K);
-    double d = 0.0, w1 = 0.0, w2 = 0.0, w3 = 0.0;
+    double d = 0.0, w1 = 0.0, w2 = 0.0, w3 = 0.0, ms = 0.0;
     bool any = false;
     const long long s2 = fb.n1, s3 = (long long)fb.n1 * fb.n2;
     for (int dk = 0; dk < 2; dk++) for (int dj = 0; dj < 2; dj++) for (int di = 0; di < 2; di++) {
         int i = 2 * I + di, j = 2 * J + dj, k = 2 * K + dk;
         if (i >= fb.n1 || j >= fb.n2 || k >= fb.n3) continue;
         long long f = fb.off + i + (long long)j * s2 + (long long)k * s3;
-        T fw1, fw2, fw3, fd;
-        if (!fine(b, f, i, j, k, fw1, fw2, fw3, fd)) continue;
+        T fw1, fw2, fw3, fd, fm;
+        if (!fine(b, f, i, j, k, fw1, fw2, fw3, fd, fm)) continue;
         any = true;
         d += fd;
+        ms += fm;
         // +x link of f: internal if di == 0, crossing to I+1 if di == 1
         if (i + 1 < fb.n1 && act(b, f + 1, i + 1, j, k)) {
             if (di == 0) d -= 2.0 * fw1;
@@ -144,18 +151,20 @@ __device__ __forceinline__ void mg_coarsen_point(const MGBlockDesc& fb, const MG
     C.w2[t] = J + 1 < cb.n2 ? (T)w2 : T(0);
     C.w3[t] = K + 1 < cb.n3 ? (T)w3 : T(0);
     C.dg[t] = any ? (T)d : T(1);
-    C.dinv[t] = any && d > 0.0 ? (T)(1.0 / d) : T(0);
+    C.mass[t] = any ? (T)ms : T(1);
+    const bool null_mode = b == MG_MAX_BLOCKS - 1 && !(d > ncut * ms);
+    C.dinv[t] = any && d > 0.0 && !null_mode ? (T)(1.0 / d) : T(0);
 }
 
 // level l+1 from the stored arrays of level l
 template <typename T>
-__global__ void mg_coarsen(MGLevelDev<T> F, MGLevelDev<T> C) {
+__global__ void mg_coarsen(MGLevelDev<T> F, MGLevelDev<T> C, double ncut) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= C.total) return;
     const int b = find_block(C, t);
-    mg_coarsen_point(F.blk[b], C.blk[b], b, t, C,
-                     [&](int, long long f, int, int, int, T& w1, T& w2, T& w3, T& d) {
-                         w1 = F.w1[f]; w2 = F.w2[f]; w3 = F.w3[f]; d = F.dg[f];
+    mg_coarsen_point(F.blk[b], C.blk[b], b, t, C, ncut,
+                     [&](int, long long f, int, int, int, T& w1, T& w2, T& w3, T& d, T& m) {
+                         w1 = F.w1[f]; w2 = F.w2[f]; w3 = F.w3[f]; d = F.dg[f]; m = F.mass[f];
                          return F.dinv[f] != T(0);
                      },
                      [&](int, long long f, int, int, int) { return F.dinv[f] != T(0); });
@@ -163,13 +172,16 @@ __global__ void mg_coarsen(MGLevelDev<T> F, MGLevelDev<T> C) {
 
 // level 1 straight from the node coefficients (level 0 keeps no arrays of its own)
 template <typename T>
-__global__ void mg_coarsen_fine(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, MGLevelDev<T> F, MGLevelDev<T> C) {
+__global__ void mg_coarsen_fine(QGrid g, QCoef<T> c, QStepPar<T> P, T vshift, MGLevelDev<T> F, MGLevelDev<T> C,
+                                double ncut) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= C.total) return;
     const int b = find_block(C, t);
-    mg_coarsen_point(F.blk[b], C.blk[b], b, t, C,
-                     [&](int bb, long long, int i, int j, int k, T& w1, T& w2, T& w3, T& d) {
-                         return mg_fine_point(g, c, P, vshift, bb, i + 1, j + 1, k + 1, w1, w2, w3, d);
+    mg_coarsen_point(F.blk[b], C.blk[b], b, t, C, ncut,
+                     [&](int bb, long long, int i, int j, int k, T& w1, T& w2, T& w3, T& d, T& m) {
+                         const bool a = mg_fine_point(g, c, P, vshift, bb, i + 1, j + 1, k + 1, w1, w2, w3, d);
+                         m = d;
+                         return a;
                      },
                      [&](int bb, long long, int i, int j, int k) { return mg_fine_active(g, bb, i + 1, j + 1, k + 1); });
 }
@@ -740,7 +752,7 @@ QmsMG<T>::~QmsMG() { release(); }
 template <typename T>
 void QmsMG<T>::release() {
     for (auto& L : lv) {
-        T* ps[] = {L.w1, L.w2, L.w3, L.dg, L.dinv, L.x, L.b, L.t};
+        T* ps[] = {L.w1, L.w2, L.w3, L.dg, L.dinv, L.x, L.b, L.t, L.mass};
         for (T* p : ps) if (p) cudaFree(p);
     }
     lv.clear();
@@ -766,7 +778,7 @@ int QmsMG<T>::levels_for(const QGrid& g, int min_coarse) {
 
 template <typename T>
 size_t QmsMG<T>::bytes_for(const QGrid& g, int min_coarse, bool tiled) {
-    // every level stores 8 values per point; a tiled level 0 (stored node coefficients,
+    // every level stores 9 values per point; a tiled level 0 (stored node coefficients,
     // more than one level) stores none: its x/b are the Krylov vectors and the caller's temporary
     long long dims[4][3] = {{g.xs, g.Ny, g.Nz}, {g.Nx, g.ys, g.Nz}, {g.Nx, g.Ny, g.zs}, {g.Nx, g.Ny, g.Nz}};
     size_t total = 0;
@@ -777,11 +789,11 @@ size_t QmsMG<T>::bytes_for(const QGrid& g, int min_coarse, bool tiled) {
             mx = std::max({mx, dims[b][0], dims[b][1], dims[b][2]});
         }
         if (mx <= min_coarse) {
-            total += (size_t)pts * 8 * sizeof(T);
+            total += (size_t)pts * 9 * sizeof(T);
             total += (size_t)4 * pts * pts * 8 / 4 + 1024;
             break;
         }
-        if (!(tiled && l == 0)) total += (size_t)pts * 8 * sizeof(T);
+        if (!(tiled && l == 0)) total += (size_t)pts * 9 * sizeof(T);
         for (int b = 0; b < 4; b++) for (int a = 0; a < 3; a++) dims[b][a] = (dims[b][a] + 1) / 2;
     }
     return total;
@@ -821,21 +833,24 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
         const size_t bytes = L.total * sizeof(T);
         CKM(cudaMalloc(&L.w1, bytes)); CKM(cudaMalloc(&L.w2, bytes)); CKM(cudaMalloc(&L.w3, bytes));
         CKM(cudaMalloc(&L.dg, bytes)); CKM(cudaMalloc(&L.dinv, bytes)); CKM(cudaMalloc(&L.t, bytes));
+        CKM(cudaMalloc(&L.mass, bytes));
         if (l > 0) { CKM(cudaMalloc(&L.x, bytes)); CKM(cudaMalloc(&L.b, bytes)); }
     }
     g0 = g; c0 = c; P0 = P; vshift0 = vshift;
     g0block = dim3(OTX, OTY, 1);
     g0grid = dim3((g.Nx + OTX - 1) / OTX, (g.Ny + OTY - 1) / OTY, (g.Nz + OKB - 1) / OKB);
-    mg_coarsen_fine<<<nblk(lv[1].total), 256, 0, st>>>(g, c, P, vshift, lv[0], lv[1]);
+    const double ncut = vcut > 0.0 ? vcut : (sizeof(T) == 8 ? 1e-9 : 1e-5);
+    mg_coarsen_fine<<<nblk(lv[1].total), 256, 0, st>>>(g, c, P, vshift, lv[0], lv[1], ncut);
     mg_mask_links<<<nblk(lv[1].total), 256, 0, st>>>(lv[1]);
     for (size_t l = tiled0 ? 2 : 1; l < lv.size(); l++) {
-        mg_coarsen<<<nblk(lv[l].total), 256, 0, st>>>(lv[l - 1], lv[l]);
+        mg_coarsen<<<nblk(lv[l].total), 256, 0, st>>>(lv[l - 1], lv[l], ncut);
         mg_mask_links<<<nblk(lv[l].total), 256, 0, st>>>(lv[l]);
     }
     CKM(cudaGetLastError());
     // coarsest level: dense inverse per block in FP64 on the host
     MGLevelDev<T>& C = lv.back();
-    std::vector<T> w1(C.total), w2(C.total), w3(C.total), dg(C.total), dinv(C.total);
+    std::vector<T> w1(C.total), w2(C.total), w3(C.total), dg(C.total), dinv(C.total), mass(C.total);
+    CKM(cudaMemcpyAsync(mass.data(), C.mass, C.total * sizeof(T), cudaMemcpyDeviceToHost, st));
     CKM(cudaMemcpyAsync(w1.data(), C.w1, C.total * sizeof(T), cudaMemcpyDeviceToHost, st));
     CKM(cudaMemcpyAsync(w2.data(), C.w2, C.total * sizeof(T), cudaMemcpyDeviceToHost, st));
     CKM(cudaMemcpyAsync(w3.data(), C.w3, C.total * sizeof(T), cudaMemcpyDeviceToHost, st));
@@ -870,11 +885,18 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
         }
         if (b == C.nb - 1) {
             // V block: pseudo-inverse.  An isolated conductor's potential is pinned only by the
-            // 1e-12 S/m floor; on the coarsest grid that is an eigenvalue ~1e-19 of the
-            // diagonally scaled operator.  Inverting it would amplify round-off without bound,
-            // so eigenvalues at or below `vcut` are dropped (the mode does not enter A or H).
+            // 1e-12 S/m floor; on the coarsest grid that is an eigenvalue ~1e-19 of the operator
+            // scaled by the summed level-0 diagonals of each point (its stiffness).  Inverting it
+            // would amplify round-off without bound, so eigenvalues at or below the cut are
+            // dropped (the mode does not enter A or H), and so are the near-null points the
+            // coarsening already took out (inactive rows).  Scaling by the point's own Galerkin
+            // diagonal instead would hide the mode: a body that collapsed into one point has a
+            // diagonal of pure rounding noise and an eigenvalue near 1 in that scaling.
             std::vector<double> dsq(m);
-            for (int r = 0; r < m; r++) dsq[r] = 1.0 / std::sqrt(std::fabs(A[(size_t)r * m + r]));
+            for (int r = 0; r < m; r++) {
+                const long long t = B.off + r;
+                dsq[r] = dinv[t] == T(0) ? 1.0 : 1.0 / std::sqrt(std::fabs((double)mass[t]));
+            }
             for (int r = 0; r < m; r++)
                 for (int q = 0; q < m; q++) A[(size_t)r * m + q] *= dsq[r] * dsq[q];
             for (int r = 0; r < m; r++)             // symmetrise round-off
@@ -889,9 +911,10 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
                     double acc = 0.0;
                     for (int e = 0; e < m; e++) {
                         const double lam = A[(size_t)e * m + e];
-                        if (lam > vcut) acc += Q[(size_t)r * m + e] * Q[(size_t)q * m + e] / lam;
+                        if (lam > ncut) acc += Q[(size_t)r * m + e] * Q[(size_t)q * m + e] / lam;
                     }
-                    Inv[(size_t)r * m + q] = dsq[r] * acc * dsq[q];
+                    const bool off_r = dinv[B.off + r] == T(0), off_q = dinv[B.off + q] == T(0);
+                    Inv[(size_t)r * m + q] = off_r || off_q ? 0.0 : dsq[r] * acc * dsq[q];
                 }
             std::memcpy(&minv[moff[b]], Inv.data(), sizeof(double) * (size_t)m * m);
             continue;
@@ -940,7 +963,7 @@ int QmsMG<T>::build(const QGrid& g, const QCoef<T>& c, const QStepPar<T>& P, T v
         V.blk[0] = lv[l].blk[3];
         V.blk[0].off = 0;
         V.total = lv[l].total - o;
-        T** ps[] = {&V.w1, &V.w2, &V.w3, &V.dg, &V.dinv, &V.x, &V.b, &V.t};
+        T** ps[] = {&V.w1, &V.w2, &V.w3, &V.dg, &V.dinv, &V.x, &V.b, &V.t, &V.mass};
         for (T** q : ps)
             if (*q) *q += o;
     }

@@ -28,6 +28,7 @@ struct MGLevelDev {
     T* x;                   // correction (levels > 0)
     T* b;                   // right-hand side (levels > 0)
     T* t;                   // Jacobi temporary
+    T* mass;                // sum of the level-0 diagonals a point aggregates (levels > 0)
 };
 
 // Optional timing of selected multigrid launches (CUDA events bracketing them on the stream):
@@ -62,7 +63,12 @@ struct QmsMG {
     QStepPar<T> P0{};
     T vshift0 = T(0);
     MgProf* prof = nullptr;
-    double vcut = 1e-9;            // coarsest V level: eigenvalues (diagonally scaled) at or below this are dropped
+    // Near-null points and modes of the V block: a coarse point whose Galerkin diagonal is at or
+    // below vcut times the summed level-0 diagonals it aggregates (a floating conductor that
+    // collapsed into it; the value is then rounding noise) leaves the hierarchy, and the coarsest
+    // V solve drops eigenvalues of its operator scaled by those sums at or below vcut.
+    // 0 = automatic: 1e-9 for an FP64 hierarchy, 1e-5 for FP32 (its cancellation noise is ~1e-7).
+    double vcut = 0.0;
     dim3 g0grid, g0block;
     std::string err;
 

@@ -709,7 +709,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
                 M.nu_coarse = desc.mg_coarse_sweeps;
                 M.nu_v = desc.mg_v_sweeps;
                 M.tail_points = desc.mg_tail_points == 0 ? 4096 : std::max(0, desc.mg_tail_points);
-                M.vcut = desc.mg_v_coarse_cut > 0.0 ? desc.mg_v_coarse_cut : 1e-9;
+                M.vcut = desc.mg_v_coarse_cut;
                 rc = M.build(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, tr == 1), vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             } else {
@@ -718,7 +718,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
                 M.nu_coarse = desc.mg_coarse_sweeps;
                 M.nu_v = desc.mg_v_sweeps;
                 M.tail_points = desc.mg_tail_points == 0 ? 4096 : std::max(0, desc.mg_tail_points);
-                M.vcut = desc.mg_v_coarse_cut > 0.0 ? desc.mg_v_coarse_cut : 1e-9;
+                M.vcut = desc.mg_v_coarse_cut;
                 rc = M.build(g, coef32(), qms_step_par<float>(g, 0, 0, 0, desc.dt, tr == 1), (float)vshift, st);
                 if (rc) { err = M.err; return QMS_ERR_CUDA; }
             }

@@ -114,9 +114,11 @@ typedef struct {
                                 3 (default) cubic, 4 x_n - 6 x_(n-1) + 4 x_(n-2) - x_(n-3);
                                 2 quadratic, 3 x_n - 3 x_(n-1) + x_(n-2); 1 linear,
                                 2 x_n - x_(n-1); 0 none */
-    double mg_v_coarse_cut;  /* coarsest multigrid level of the potential block: eigenvalues of its
-                                diagonally scaled operator at or below this are dropped from its
-                                pseudo-inverse (0 = automatic: 1e-9) */
+    double mg_v_coarse_cut;  /* near-null modes of the potential block's multigrid: a coarse point whose
+                                Galerkin diagonal is at or below this times the summed level-0
+                                diagonals it aggregates leaves the hierarchy, and the coarsest solve
+                                drops eigenvalues of its operator scaled by those sums at or below
+                                it (0 = automatic: 1e-9 with FP64 inner vectors, 1e-5 with FP32) */
 } qms_desc;
 
 typedef struct {
