@@ -126,6 +126,10 @@ SIGNATURES = [
     ("qms_get_stats", ctypes.c_int, [_H, ctypes.POINTER(QmsStats)]),
     ("qms_wait_selftest", ctypes.c_int, [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_uint)]),
     ("qms_get_fields", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP]),
+    ("qms_get_fields_async", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, ctypes.c_int]),
+    ("qms_fields_sync", ctypes.c_int, [_H, ctypes.c_int]),
+    ("qms_pinned_alloc", ctypes.c_void_p, [ctypes.c_size_t]),
+    ("qms_pinned_free", None, [ctypes.c_void_p]),
     ("qms_get_state", ctypes.c_int, [_H, _VP]),
     ("qms_get_rhs", ctypes.c_int, [_H, _VP]),
     ("qms_set_state", ctypes.c_int, [_H, _VP]),

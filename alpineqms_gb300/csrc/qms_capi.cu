@@ -191,6 +191,27 @@ int qms_wait_selftest(qms_handle* h, int spins, unsigned* status_out) {
     return 0;
 }
 
+int qms_get_fields_async(qms_handle* h, int which, int axis, int index, double* out, int slot) {
+    HCHECK(h);
+    if (!out) { h->s.err = "null argument"; return QMS_ERR_ARG; }
+    return h->s.fields_async(which, axis, index, out, slot);
+}
+
+int qms_fields_sync(qms_handle* h, int slot) {
+    HCHECK(h);
+    return h->s.fields_sync(slot);
+}
+
+void* qms_pinned_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0 || cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void qms_pinned_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
 int qms_get_fields(qms_handle* h, int which, int axis, int index, double* out) {
     HCHECK(h);
     if (!out) { h->s.err = "null argument"; return QMS_ERR_ARG; }

@@ -514,6 +514,17 @@ void QmsSolver::release() {
     drop_graphs();
     for (auto& e : evpool) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     evpool.clear();
+    for (int q = 0; q < kFieldSlots; q++) {
+        if (fev_done[q]) cudaEventSynchronize(fev_done[q]);
+        if (fev_ready[q]) cudaEventDestroy(fev_ready[q]);
+        if (fev_done[q]) cudaEventDestroy(fev_done[q]);
+        if (fbuf[q]) cudaFree(fbuf[q]);
+        fev_ready[q] = fev_done[q] = nullptr;
+        fbuf[q] = nullptr;
+        fbuf_n[q] = 0;
+    }
+    if (cst) cudaStreamDestroy(cst);
+    cst = nullptr;
     if (st && own_stream) cudaStreamDestroy(st);
     ids = nullptr; dtab64 = nullptr; dtab32 = nullptr; x = b = r64 = H = slicebuf = part = S = nullptr;
     status = nullptr; dg_steady = dg_tr = nullptr; hS = nullptr; st = nullptr; mgtmp = nullptr; mgtmp2 = nullptr; xbest = nullptr;
@@ -1463,6 +1474,54 @@ int QmsSolver::fields(int which, int axis, int index, double* host_out) {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     return 0;
+}
+
+int QmsSolver::fields_async(int which, int axis, int index, double* host_out, int slot) {
+    CK(cudaSetDevice(dev));
+    if (slot < 0 || slot >= kFieldSlots) { err = "field slot out of range"; return QMS_ERR_ARG; }
+    const long long ncell = (long long)g.xs * g.ys * g.zs;
+    long long m = 3 * ncell;
+    if (which == QMS_FIELD_SLICE) {
+        int lim = axis == 0 ? g.xs : axis == 1 ? g.ys : g.zs;
+        if (axis < 0 || axis > 2 || index < 1 || index > lim) { err = "slice axis/index out of range"; return QMS_ERR_ARG; }
+        m = 3LL * (axis == 0 ? g.ys : g.xs) * (axis == 2 ? g.ys : g.zs);
+    } else if (which != QMS_FIELD_CUBES) {
+        err = "unknown field kind";
+        return QMS_ERR_ARG;
+    }
+    if (!cst) CK(cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking));
+    if (!fev_ready[slot]) {
+        CK(cudaEventCreateWithFlags(&fev_ready[slot], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&fev_done[slot], cudaEventDisableTiming));
+    }
+    // the slot's previous copy must be finished before its device buffer is reused
+    CK(cudaEventSynchronize(fev_done[slot]));
+    if (fbuf_n[slot] < (size_t)m) {
+        if (fbuf[slot]) CK(cudaFree(fbuf[slot]));
+        fbuf[slot] = nullptr;
+        fbuf_n[slot] = 0;
+        CK(cudaMalloc(&fbuf[slot], m * 8));
+        fbuf_n[slot] = (size_t)m;
+    }
+    double* d = fbuf[slot];
+    if (which == QMS_FIELD_CUBES)
+        qms_launch_hfield(g, ids, dtab64, x, d, d + ncell, d + 2 * ncell, st);
+    else
+        qms_launch_hslice(g, ids, dtab64, x, axis, index, d, st);
+    nlaunch++;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(fev_ready[slot], st));
+    CK(cudaStreamWaitEvent(cst, fev_ready[slot], 0));
+    CK(cudaMemcpyAsync(host_out, d, m * 8, cudaMemcpyDeviceToHost, cst));
+    CK(cudaEventRecord(fev_done[slot], cst));
+    return 0;
+}
+
+int QmsSolver::fields_sync(int slot) {
+    if (slot < 0 || slot >= kFieldSlots) return QMS_ERR_ARG;
+    if (!fev_done[slot]) return 0;
+    cudaError_t e = cudaEventSynchronize(fev_done[slot]);
+    return e == cudaSuccess ? 0 : QMS_ERR_CUDA;
 }
 
 template int QmsSolver::inner_bicgstab<float>(bool, bool, const double*, int&);

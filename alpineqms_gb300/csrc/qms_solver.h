@@ -154,6 +154,16 @@ struct QmsSolver {
     // exact: the FP64 residual even where the double-float one would do (the public entry point)
     int residual(bool adv, bool transient, const double v[3], bool exact = false);
     int fields(int which, int axis, int index, double* host_out);
+    // Asynchronous field output: H (cubes or slice) formed on the solver stream into the device
+    // buffer of `slot`, copied to host_out on a copy stream that overlaps the solver's next work;
+    // fields_sync(slot) waits for that copy (callable from another host thread).
+    static constexpr int kFieldSlots = 4;
+    cudaStream_t cst = nullptr;
+    cudaEvent_t fev_ready[kFieldSlots] = {}, fev_done[kFieldSlots] = {};
+    double* fbuf[kFieldSlots] = {};
+    size_t fbuf_n[kFieldSlots] = {};
+    int fields_async(int which, int axis, int index, double* host_out, int slot);
+    int fields_sync(int slot);
     int finalize(int op, int nsum, long long nb);
     int read_scalars();
 

@@ -101,6 +101,21 @@ class QMSSolver:
               "qms_get_fields")
         return [out[q * m:(q + 1) * m].reshape((n1, n2), order="F") for q in range(3)]
 
+    def slice_shape(self, axis: str):
+        n1 = self.ys if axis == "x" else self.xs
+        n2 = self.ys if axis == "z" else self.zs
+        return n1, n2
+
+    def fields_async(self, which: int, axis: str, index: int, out: "PinnedBuffer", slot: int):
+        """Start forming H (cubes, or the slice of `axis`/`index`) and copying it into `out`
+        without waiting; the copy overlaps the handle's next calls.  fields_sync(slot) waits."""
+        check(self.L.qms_get_fields_async(self.h, which, AXES.get(axis, 0), index, out.ptr, slot), self.h,
+              "qms_get_fields_async")
+
+    def fields_sync(self, slot: int):
+        """Waits for the copy of `slot` (may be called from another thread)."""
+        check(self.L.qms_fields_sync(self.h, slot), self.h, "qms_fields_sync")
+
     def get_state(self) -> np.ndarray:
         x = np.empty(self.n, np.float64)
         check(self.L.qms_get_state(self.h, x.ctypes.data), self.h, "qms_get_state")
@@ -145,3 +160,27 @@ class QMSSolver:
 
     def csr_spmv(self, d_ia, d_ja, d_a, d_x, d_y):
         check(self.L.qms_csr_spmv(self.h, d_ia, d_ja, d_a, d_x, d_y), self.h, "qms_csr_spmv")
+
+
+class PinnedBuffer:
+    """Page-locked host memory (qms_pinned_alloc) seen as a float64 numpy array."""
+
+    def __init__(self, n: int):
+        self.L = _lib.load()
+        self.n = int(n)
+        self.ptr = self.L.qms_pinned_alloc(self.n * 8)
+        if not self.ptr:
+            raise MemoryError(f"qms_pinned_alloc({self.n * 8}) failed")
+        self.array = np.ctypeslib.as_array(ctypes.cast(self.ptr, ctypes.POINTER(ctypes.c_double)), shape=(self.n,))
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.array = None
+            self.L.qms_pinned_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -166,6 +166,19 @@ int qms_wait_selftest(qms_handle* h, int spins, unsigned* status_out);
  * which = QMS_FIELD_SLICE: out = the three slices (axis 0/1/2 = x/y/z, 1-based
  * index), each in the record layout of F:1380-1394. */
 int qms_get_fields(qms_handle* h, int which, int axis, int index, double* out);
+/* The same fields without waiting (the per-step dumps of F:2274-2300, overlapped with the next
+ * step): H is formed on the handle's stream into the device buffer of `slot` (0..3) and copied
+ * to `out` on a separate copy stream, so the handle's next calls (qms_step ...) run while the
+ * copy is in flight.  `out` should be pinned host memory (qms_pinned_alloc) for the copy to be
+ * asynchronous, and must stay untouched until qms_fields_sync(h, slot) has returned.  A slot's
+ * next use waits for its previous copy. */
+int qms_get_fields_async(qms_handle* h, int which, int axis, int index, double* out, int slot);
+/* Waits until the copy issued on `slot` has landed.  Unlike the other calls on a handle, it may
+ * be made from another host thread while the owning thread keeps stepping. */
+int qms_fields_sync(qms_handle* h, int slot);
+/* Page-locked host memory for qms_get_fields_async (NULL on failure) and its release. */
+void* qms_pinned_alloc(size_t bytes);
+void qms_pinned_free(void* p);
 int qms_get_state(qms_handle* h, double* x_out);          /* n_dims doubles */
 int qms_get_rhs(qms_handle* h, double* b_out);            /* n_dims doubles: the right-hand side of the last
                                                              solve (RHS of F:1457-2191, Dirichlet values
