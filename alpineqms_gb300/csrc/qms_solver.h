@@ -7,6 +7,7 @@
 #include "qms_df.cuh"
 
 #include <algorithm>
+#include <deque>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -120,7 +121,9 @@ struct QmsSolver {
     OpEv* prof_begin(int kind, double bytes);
     void prof_end(OpEv* ev);
     bool prof_accum(const OpEv& e);              // false when the events cannot be timed
-    std::vector<OpEv> evpool;
+    // a deque: prof_begin hands out pointers into it that stay valid while later events are
+    // added (profile events nest: the A-block sweeps inside a V-cycle's own event)
+    std::deque<OpEv> evpool;
     size_t evused = 0;
     bool capturing = false;                      // event records go into a graph being captured
     bool graph_prof_broken = false;
@@ -185,7 +188,7 @@ struct QmsSolver {
         bool resid_df = false;      // the captured residual is the double-float one (rfin)
         double v[3] = {0, 0, 0};
         long long launches = 0;
-        std::vector<OpEv> ev;
+        std::deque<OpEv> ev;
         size_t evn = 0;
         unsigned long long used = 0;
     };
