@@ -147,23 +147,24 @@ WORKLOADS = {
 
 def inputs_text(inp: QMSInputs) -> str:
     """inputs.txt in the positional grammar of 3D/master.py:23-66."""
-    L = [f"{inp.xs},{inp.ys},{inp.zs}", f"{inp.dx!r},{inp.dy!r},{inp.dz!r}", repr(inp.dt), str(inp.nt),
-         str(inp.tt), f"{inp.slice_axis},{inp.slice_index}", inp.save_all,
-         "{!r},{!r},{!r}".format(*inp.B)]
+    def r3(v):     # plain Python floats: numpy scalars would print as np.float64(...)
+        return "{!r},{!r},{!r}".format(*(float(a) for a in v))
+    L = [f"{inp.xs},{inp.ys},{inp.zs}", r3((inp.dx, inp.dy, inp.dz)), repr(float(inp.dt)), str(inp.nt),
+         str(inp.tt), f"{inp.slice_axis},{inp.slice_index}", inp.save_all, r3(inp.B)]
     for row in inp.G:
-        L.append("{!r},{!r},{!r}".format(*row))
+        L.append(r3(row))
     for t in inp.traj:
         L.append(str(t.kind))
-        L.append(f"{t.v0!r},{t.accel!r},{t.n_accel}")
+        L.append(f"{float(t.v0)!r},{float(t.accel)!r},{int(t.n_accel)}")
     L.append(str(len(inp.materials)))
     for m in inp.materials:
         L.append(repr(float(m.mat_id)))
-        L.append("{!r},{!r},{!r}".format(*m.mu_r))
-        L.append("{!r},{!r},{!r}".format(*m.sigma))
+        L.append(r3(m.mu_r))
+        L.append(r3(m.sigma))
     L.append(inp.geom_name)
     if inp.excitation is not None:
         k, f, ph = inp.excitation
-        L.append(f"excitation,{k},{f!r},{ph!r}")
+        L.append(f"excitation,{k},{float(f)!r},{float(ph)!r}")
     return "\n".join(L) + "\n"
 
 

@@ -256,7 +256,8 @@ def test_dropin_dumps_vs_reference_program(name, tmp_path):
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_plain_block_32_twenty_steps(precision):
     """The 32^3 copper block under a 1 kHz field (steady + 20 steps): every z-mid H
-    slice record within 1e-8 relative L2 of the oracle's direct solve
+    slice record, and the whole A block, edge current sigma grad V and H cubes at the
+    fixture's full steps, within 1e-8 relative L2 of the oracle's direct solve
     (tests/golden/plain_block_32.npz, made by tests/golden/make_config1.py)."""
     from alpineqms_gb300 import workloads
     from alpineqms_gb300.trajectory import VelocitySchedule, scaled_field
@@ -275,8 +276,17 @@ def test_plain_block_32_twenty_steps(precision):
         assert rel_l2(got, z["slices"][n]) <= 1e-8, (n, rel_l2(got, z["slices"][n]))
         hn = np.sqrt(sum(np.dot(h.ravel(), h.ravel()) for h in H))
         assert abs(hn - z["hnorm"][n]) <= 1e-8 * z["hnorm"][n], (n, hn, z["hnorm"][n])
-        xa = s.get_state()[:o.block_offsets(inp.xs, inp.ys, inp.zs)[3]]
+        x = s.get_state()
+        xa = x[:o.block_offsets(inp.xs, inp.ys, inp.zs)[3]]
         assert abs(np.linalg.norm(xa) - z["anorm"][n]) <= 1e-8 * z["anorm"][n]
+        if n in set(int(q) for q in z["full_steps"]):
+            # whole vectors at these steps: A, the edge current sigma grad V and the H cubes
+            c = o.materials(inp.xs, inp.ys, inp.zs, geom, inp.props_table())
+            j = o.edge_current_from_v(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, c, x)
+            assert rel_l2(xa, z["a_%d" % n]) <= 1e-8, (n, rel_l2(xa, z["a_%d" % n]))
+            assert rel_l2(j, z["j_%d" % n]) <= 1e-8, (n, rel_l2(j, z["j_%d" % n]))
+            h = np.concatenate([q.ravel(order="F") for q in H])
+            assert rel_l2(h, z["h_%d" % n]) <= 1e-8, (n, rel_l2(h, z["h_%d" % n]))
     s.close()
 
 
