@@ -1365,6 +1365,12 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
             const double lgoal = std::log(0.5 * desc.tol / rel);
             if (graph_cycles >= 2 && gm_lrate[1] < -1e-3 && lgoal < 0.0)
                 it = std::min(gm_m, std::max(6, (int)std::ceil(lgoal / gm_lrate[1]) + 2));
+            // a start residual that the usual count would leave just above the tolerance: one
+            // cycle a few steps longer (at the observed first-cycle rate) instead of two cycles
+            if (graph_cycles == 0 && desc.gm_first_extend > 0 && gm_lrate[0] < -1e-3 && lgoal < 0.0) {
+                const int need = (int)std::ceil(lgoal / gm_lrate[0]) + 1;
+                if (need > it && need <= std::min(gm_m, gm_k_est + desc.gm_first_extend)) it = need;
+            }
             graph_cycles++;
             rc = ir_iteration_graph(adv, transient, v, it);
             if (rc) return rc;

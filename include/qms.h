@@ -119,6 +119,10 @@ typedef struct {
                                 diagonals it aggregates leaves the hierarchy, and the coarsest solve
                                 drops eigenvalues of its operator scaled by those sums at or below
                                 it (0 = automatic: 1e-9 with FP64 inner vectors, 1e-5 with FP32) */
+    int gm_first_extend;     /* replayed refinement iterations: the first FGMRES cycle of a solve may run
+                                up to this many steps beyond the learned count when the start residual
+                                and the observed first-cycle rate say that one cycle then reaches the
+                                tolerance (instead of two cycles); 0 = never (default 3) */
 } qms_desc;
 
 typedef struct {
