@@ -26,6 +26,8 @@
 #include "qms_pl.h"
 #include "qms_tile.cuh"
 
+#include <cuda_bf16.h>
+
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -466,16 +468,25 @@ template <int QS> struct MG0Set {
     static constexpr bool A = QS != 2, V = QS != 1;
 };
 
+// Coefficient tiles of the level-0 kernels: bf16 in an FP32 hierarchy (a preconditioner needs
+// no more than its ~3 significant digits, and the six node coefficients are 40 % of a sweep's
+// DRAM traffic in FP32), the hierarchy's own type in FP64.
+template <typename T> struct MG0Coef { using type = T; };
+template <> struct MG0Coef<float> { using type = __nv_bfloat16; };
+__device__ __forceinline__ float mg_cf(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ double mg_cf(double v) { return v; }
+
 template <typename T, int KIND, int QS>
 __global__ void __launch_bounds__(OTX * OTY, sizeof(T) == 4 ? QMS_STENCIL_MINB : 2)
 mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __restrict__ b, int scaled,
           const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap, T* __restrict__ xout,
           MGLevelDev<T> C, T* __restrict__ bc, unsigned* __restrict__ err) {
     using S = MG0Set<QS>;
-    using TL = PLTiles<T, S::NQ, S::NC>;
+    using CT = typename MG0Coef<T>::type;
+    using TL = PLTiles<T, S::NQ, S::NC, CT>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* xsm = reinterpret_cast<T*>(smem_raw);                  // [4 slots][NQ][PLXY][PLX]
-    T* csm = xsm + 4 * TL::XSLOT;                             // [3 slots][NC][PLCY][PLX]
+    CT* csm = reinterpret_cast<CT*>(smem_raw + 4 * TL::XSLOT * sizeof(T));   // [3 slots][NC][PLCY][CX]
     __shared__ __align__(8) uint64_t xbar[4], cbar[3];
     __shared__ T red[KIND == 2 ? S::NQ : 1][OTY][OTX];
     constexpr bool STAGE = KIND != 0;
@@ -554,11 +565,12 @@ mg0_tiled(QGrid g, QStepPar<T> P, T vshift, T omega, int mask_v, const T* __rest
         const T* xm = xsm + ((k - 1) & 3) * TL::XSLOT;
         const T* x0 = xsm + (k & 3) * TL::XSLOT;
         const T* xp = xsm + ((k + 1) & 3) * TL::XSLOT;
-        const T* cprv = csm + ((k - 1) % 3) * TL::CSLOT;
-        const T* ccur = csm + (k % 3) * TL::CSLOT;
+        const CT* cprv = csm + ((k - 1) % 3) * TL::CSLOT;
+        const CT* ccur = csm + (k % 3) * TL::CSLOT;
         const bool kfA = k <= 2 || k >= g.Nz - 1;       // k terms of qFixX / qFixY / qFixV
         const bool kfZ = k == 1 || k == g.zs;           // k term of qFixZ
-#define CF(q, dk, dj, di) (dk < 0 ? cprv : ccur)[((q) - S::C0) * PLCY * PLX + (lj + (dj)) * PLX + li + (di)]
+#define CF(q, dk, dj, di) \
+    ((T)mg_cf((dk < 0 ? cprv : ccur)[((q) - S::C0) * PLCY * TL::CX + (lj + (dj)) * TL::CX + li + (di)]))
 #define XS(q, sl, dj, di) (sl)[((q) - S::Q0) * PLXY * PLX + (lj + (dj)) * PLX + li + (di)]
         T r[4] = {T(0), T(0), T(0), T(0)};
         // one component: links (wxp, wxm, wyp, wym, wzp, wzm), extra diagonal
@@ -668,7 +680,7 @@ __global__ void mg0_prolong(QGrid g, int mask_v, T* __restrict__ x, MGLevelDev<T
 
 template <typename T, int KIND, int QS = 0>
 static size_t mg0_smem() {
-    return PLTiles<T, MG0Set<QS>::NQ, MG0Set<QS>::NC>::SMEM;
+    return PLTiles<T, MG0Set<QS>::NQ, MG0Set<QS>::NC, typename MG0Coef<T>::type>::SMEM;
 }
 
 // raise the dynamic shared-memory limit of the level-0 kernels once per device

@@ -70,6 +70,39 @@ bool qms_make_pl_map(CUtensorMap* map, const void* base, const QGrid& g, int ele
     return r == CUDA_SUCCESS;
 }
 
+bool qms_make_pl16_map(CUtensorMap* map, const void* base, const QGrid& g, int arrays) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return false;
+    const long long P16 = qms_pl16_pitch(g);
+    const cuuint64_t dims[4] = {(cuuint64_t)P16, (cuuint64_t)g.Ny, (cuuint64_t)g.Nz, (cuuint64_t)arrays};
+    const cuuint64_t strides[3] = {(cuuint64_t)P16 * 2, (cuuint64_t)P16 * g.Ny * 2, (cuuint64_t)P16 * g.Ny * g.Nz * 2};
+    const cuuint32_t box[4] = {PLX16, (cuuint32_t)PLCY, 1, (cuuint32_t)arrays};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+// the bf16 copy of the FP32 node coefficients (padding stays zero: the caller clears it)
+__global__ void qk_coef_bf16(QGrid g, const float* __restrict__ nc, __nv_bfloat16* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.Nx || j > g.Ny) return;
+    const QPL L = qms_pl(g);
+    const long long src = qms_pl_node(g, L, i, j, k);
+    const long long P16 = qms_pl16_pitch(g), comp16 = P16 * g.Ny * g.Nz;
+    const long long dst = ((long long)(k - 1) * g.Ny + (j - 1)) * P16 + i;
+#pragma unroll
+    for (int q = 0; q < 6; q++) out[q * comp16 + dst] = __float2bfloat16_rn(nc[q * L.comp + src]);
+}
+
+void qms_launch_coef_bf16(const QGrid& g, const float* nc, __nv_bfloat16* out, cudaStream_t st) {
+    const long long P16 = qms_pl16_pitch(g);
+    cudaMemsetAsync(out, 0, 6 * P16 * g.Ny * g.Nz * sizeof(__nv_bfloat16), st);
+    qk_coef_bf16<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, nc, out);
+}
+
 // ---------------------------------------------------------------------------
 // operator on the padded layout
 // ---------------------------------------------------------------------------

@@ -4,6 +4,8 @@
 #include "qms_tma.cuh"
 #include "qms_df.cuh"
 
+#include <cuda_bf16.h>
+
 // one thread per node: blocks of QMS_NODE_BX (along x) x QMS_NODE_BY (along y) nodes of a plane
 #define QMS_NODE_BX 32
 #define QMS_NODE_BY 16
@@ -66,6 +68,9 @@ void qms_launch_pl_scale(long long n, const float* r, const double* scale, float
 
 // one CTA waiting (at most `spins` polls) on an mbarrier that never completes: sets QMS_ST_TIMEOUT
 void qms_launch_wait_selftest(int spins, unsigned* err, cudaStream_t st);
+
+// the bf16 copy (qms_pl16_pitch rows) of the FP32 node coefficients, for the multigrid's level 0
+void qms_launch_coef_bf16(const QGrid& g, const float* nc, __nv_bfloat16* out, cudaStream_t st);
 
 void qms_launch_diag_pl(const QGrid& g, const QCoef<float>& c, const QStepPar<float>& P, float* dg, cudaStream_t st);
 

@@ -505,6 +505,8 @@ void QmsSolver::release() {
     if (gm_H) cudaFree(gm_H);
     if (gm_scal) cudaFree(gm_scal);
     gm_H = gm_scal = nullptr;
+    if (nc16) cudaFree(nc16);
+    nc16 = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
                     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
                     rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2, hist_x, xold3, wh[0], wh[1], wh[2]};
@@ -646,6 +648,14 @@ int QmsSolver::init(const qms_desc& d) {
         tmapsA[p] = ma;
         tmapsV[p] = mv;
     }
+    if (!fp64_inner) {
+        const long long comp16 = (long long)qms_pl16_pitch(g) * g.Ny * g.Nz;
+        CK(cudaMalloc(&nc16, 6 * comp16 * sizeof(__nv_bfloat16)));
+        if (!qms_make_pl16_map(&cmap16, nc16, g, 6) || !qms_make_pl16_map(&cmapV16, nc16 + 3 * comp16, g, 3)) {
+            err = "tensor map encoding failed";
+            return QMS_ERR_CUDA;
+        }
+    }
     const long long cv = 3 * qms_pl(g).comp;                          // first conductivity array
     if (!qms_make_pl_map(&cmap32, nc32, g, 4, 6, PLCY) || !qms_make_pl_map(&cmap64, nc64, g, 8, 6, PLCY) ||
         !qms_make_pl_map(&cmapV32, nc32 + cv, g, 4, 3, PLCY) || !qms_make_pl_map(&cmapV64, nc64 + cv, g, 8, 3, PLCY)) {
@@ -662,6 +672,7 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     // the block-triangular preconditioner's V right-hand side; the double-float residual's x, b,
     // coefficients and FP32 result (mixed precision)
     size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
+    if (ts == 4) tri += (size_t)6 * qms_pl16_pitch(g) * g.Ny * g.Nz * 2;       // bf16 node coefficients
     if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4 + 8 + 8) + 6 * qms_pl(g).comp * 8 + 5 * g.n * 8 + 2 * g.oV * 8 +
                         (d.extrapolate >= 3 ? g.n * 8 : 0) + std::max(0, std::min(d.extrapolate, 3)) * qms_pl(g).n * 8;
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
@@ -699,6 +710,7 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     // node coefficients, then the Jacobi diagonals (velocity does not enter the diagonal)
     qms_launch_node_coef<float>(g, coef32(), nc32, st);
     qms_launch_node_coef<double>(g, coef64(), nc64, st);
+    if (nc16) qms_launch_coef_bf16(g, nc32, nc16, st);
     if (df_resid) qms_launch_split_flat(6 * qms_pl(g).comp, nc64, ncdf, st);
     if (rsg) qms_launch_rhs_coef(g, ids, dtab64, desc.dt, rsg, rsdt, st);
     if (dinvdf) qms_launch_dinv_df(g, coef64(), qms_step_par<double>(g, 0, 0, 0, desc.dt, true), dinvdf, st);
@@ -865,7 +877,8 @@ void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool
     if (use_mg) {
         OpEv* ev = prof_begin(2, 0.0);
         const bool f32 = sizeof(T) == 4;
-        const CUtensorMap& cm = f32 ? cmap32 : cmap64;
+        // the cycles' level-0 tiles read the bf16 coefficients in an FP32 hierarchy
+        const CUtensorMap& cm = f32 ? cmap16 : cmap64;
         auto cycle = [&](const T* b, int qs, const CUtensorMap& cmq) {
             // b's own tile map for the fused first sweeps of the subset cycles (a mapped vector)
             const CUtensorMap* bm = nullptr;
@@ -889,7 +902,7 @@ void QmsSolver::precond(const T* r, const float* bscale, T* z, bool mask_v, bool
             cycle(r, 1, cm);
             qms_launch_op_pl<T>(g, *P, tmapq(z, 1), f32 ? cmapV32 : cmapV64, adv, QOPH_VCOUPLE, tv, r, nullptr,
                                 status, st);
-            cycle(tv, 2, f32 ? cmapV32 : cmapV64);
+            cycle(tv, 2, f32 ? cmapV16 : cmapV64);
             nlaunch++;
             regions.apply<T>(tv, bscale, z, st, nlaunch);
         } else {

@@ -6,6 +6,8 @@
 #include "qms_tma.cuh"
 #include "qms_df.cuh"
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <deque>
 #include <string>
@@ -146,6 +148,9 @@ struct QmsSolver {
     CUtensorMap cmap32{}, cmap64{};                 // ... and of the node coefficients
     std::unordered_map<const void*, CUtensorMap> tmapsA, tmapsV;   // ... of their A blocks / V block
     CUtensorMap cmapV32{}, cmapV64{};               // ... of the three conductivities
+    // bf16 copy of the FP32 node coefficients (the multigrid's level-0 tiles) and its maps
+    __nv_bfloat16* nc16 = nullptr;
+    CUtensorMap cmap16{}, cmapV16{};
     const CUtensorMap& tmap(const void* p) const;
     const CUtensorMap& tmapq(const void* p, int qs) const;
 

@@ -96,18 +96,27 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
 // NC arrays (all six, or the three conductivities), rows j0-1 .. j0+7.  Slots are padded to
 // 128 bytes.
 #define PLX 36
+#define PLX16 40      // 2-byte elements: a row of the box must be a multiple of 16 bytes (80 B)
 #define PLXY 10
 #define PLCY 9
-template <typename T, int NQ = 4, int NC = 6>
+// CT: element type of the coefficient tiles (2-byte coefficients use PLX16 columns)
+template <typename T, int NQ = 4, int NC = 6, typename CT = T>
 struct PLTiles {
+    static constexpr int CX = sizeof(CT) == 2 ? PLX16 : PLX;             // coefficient tile row width
     static constexpr int XSLOT_RAW = NQ * PLXY * PLX;                     // elements per x plane
     static constexpr int XSLOT = ((XSLOT_RAW * (int)sizeof(T) + 127) / 128) * 128 / (int)sizeof(T);
-    static constexpr int CSLOT_RAW = NC * PLCY * PLX;
-    static constexpr int CSLOT = ((CSLOT_RAW * (int)sizeof(T) + 127) / 128) * 128 / (int)sizeof(T);
+    static constexpr int CSLOT_RAW = NC * PLCY * CX;
+    static constexpr int CSLOT = ((CSLOT_RAW * (int)sizeof(CT) + 127) / 128) * 128 / (int)sizeof(CT);
     static constexpr unsigned XBYTES = XSLOT_RAW * sizeof(T);
-    static constexpr unsigned CBYTES = CSLOT_RAW * sizeof(T);
-    static constexpr size_t SMEM = (size_t)(4 * XSLOT + 3 * CSLOT) * sizeof(T);
+    static constexpr unsigned CBYTES = CSLOT_RAW * sizeof(CT);
+    static constexpr size_t SMEM = (size_t)4 * XSLOT * sizeof(T) + (size_t)3 * CSLOT * sizeof(CT);
 };
+
+// the 2-byte copy of the node coefficients: the same [6][Nz][Ny][P16] order with rows of
+// P16 = Nx + 1 rounded up to a multiple of 8 (16-byte rows for a tensor map)
+__host__ __device__ __forceinline__ int qms_pl16_pitch(const QGrid& g) { return (g.Nx + 1 + 7) & ~7; }
 
 // host: tensor maps of a padded vector (4 blocks) and of the padded node coefficients (6 arrays)
 bool qms_make_pl_map(CUtensorMap* map, const void* base, const QGrid& g, int elem_bytes, int arrays, int box_rows);
+// ... and of the bf16 copy of the node coefficients (`arrays` of them from base, PLX16 x PLCY boxes)
+bool qms_make_pl16_map(CUtensorMap* map, const void* base, const QGrid& g, int arrays);
