@@ -53,7 +53,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->mg_alpha = 1.5;
     d->mg_coupling = 1;
     d->extrapolate = 3;
-    d->gm_first_extend = 3;
+    d->gm_first_extend = 0;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }

@@ -122,7 +122,8 @@ typedef struct {
     int gm_first_extend;     /* replayed refinement iterations: the first FGMRES cycle of a solve may run
                                 up to this many steps beyond the learned count when the start residual
                                 and the observed first-cycle rate say that one cycle then reaches the
-                                tolerance (instead of two cycles); 0 = never (default 3) */
+                                tolerance (instead of two cycles); 0 = never (the default: on the
+                                moving plate it kept longer single cycles, 30.6 vs 28.0 ms per step) */
 } qms_desc;
 
 typedef struct {
