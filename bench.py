@@ -58,6 +58,8 @@ def parse_args():
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the plain FP64 GPU solver leg (its timing and the per-step comparison)")
     ap.add_argument("--workload", default="moving_plate_256", choices=WORKLOADS)
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="steps of the kernel-timing pass (0: as many as the timed steps)")
     ap.add_argument("--fp64-steps", type=int, default=0,
                     help="steps of the FP64 leg (0: the warm-up and timed steps; fewer for grids whose FP64 "
                          "solve takes seconds per step)")
@@ -363,10 +365,11 @@ def run_gpu(args):
     torch.cuda.synchronize()
     run.s.profile_enable(True)          # counts from here
     ext = torch.cuda.ExternalStream(run.s.stream_ptr())
-    prof_ms, _ = timed_steps(run, K, ext)
+    KP = args.profile_steps if args.profile_steps > 0 else K
+    prof_ms, _ = timed_steps(run, KP, ext)
     prof = run.s.profile()
     run.s.profile_enable(False)
-    prof_ms_per_step = prof_ms / K
+    prof_ms_per_step = prof_ms / KP
     run.close()
 
     # -- 4. the plain FP64 GPU solver (the same algorithm with every inner component in FP64, the
@@ -448,7 +451,7 @@ def run_gpu(args):
                 "avg_launch_us": 1e3 * kms / max(klaunch, 1),
                 "algorithmic_bytes_per_launch": kbytes / max(klaunch, 1),
                 "algorithmic_bytes_def": "3 p n_A + cells (x and b read, x written; one material byte per cell)",
-                "share_of_step": kms / (prof_ms_per_step * K) if prof_ms_per_step > 0 else None,
+                "share_of_step": kms / (prof_ms_per_step * KP) if prof_ms_per_step > 0 else None,
                 "timed_pass": "kernel timings from a later pass of as many steps with CUDA events around the "
                               "timed launches (%.2f ms per step there)" % prof_ms_per_step,
                 "other_kernels_ms": {"op32": prof["op32_ms"], "op64": prof["op64_ms"], "vcycles": prof["mg_ms"],
