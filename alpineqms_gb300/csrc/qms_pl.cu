@@ -361,17 +361,27 @@ struct QStartRhs {
     qdf idt[3];                     // 1 / (dt dx), 1 / (dt dy), 1 / (dt dz)
     double* x0;                     // receives x_n
 };
+// dp (optional): the pointers of the history buffers that rotate from step to step, read from
+// device memory instead of the arguments (a step captured in a CUDA graph replays with the
+// pointers of the step it runs)
 __global__ void __launch_bounds__(256) qk_step_start(
-    QGrid g, qdf* __restrict__ rfin, const double* __restrict__ b, const double* __restrict__ bprev,
-    const qdf* __restrict__ dinv, qdf* __restrict__ r0, double* __restrict__ x, const double* __restrict__ xo1,
-    const double* __restrict__ xo2, const double* __restrict__ xo3, const int xo, qdf* __restrict__ wnew,
-    const qdf* __restrict__ w1, const qdf* __restrict__ w2, float* __restrict__ rfloat,
-    double* __restrict__ partials, const QStartRhs R) {
+    QGrid g, qdf* __restrict__ rfin, const double* b_a, const double* bprev_a, const qdf* __restrict__ dinv,
+    qdf* __restrict__ r0, double* __restrict__ x, const double* xo1_a, const double* xo2_a, const double* xo3_a,
+    const int xo, qdf* wnew_a, const qdf* w1_a, const qdf* w2_a, float* __restrict__ rfloat,
+    double* __restrict__ partials, const QStartRhs R, const QStepPtrs* __restrict__ dp) {
     __shared__ qdf prod[3][64];
     const QPL L = qms_pl(g);
     const int c = threadIdx.x >> 6, lane = threadIdx.x & 63;
     const unsigned Nx = (unsigned)g.Nx, Nxy = (unsigned)g.Nx * (unsigned)g.Ny, Nn = (unsigned)g.Nn;
-    const double* __restrict__ hx = R.hx;
+    const double* __restrict__ b = dp ? dp->b : b_a;
+    const double* __restrict__ bprev = dp ? dp->bprev : bprev_a;
+    const double* __restrict__ xo1 = dp ? dp->xo1 : xo1_a;
+    const double* __restrict__ xo2 = dp ? dp->xo2 : xo2_a;
+    const double* __restrict__ xo3 = dp ? dp->xo3 : xo3_a;
+    qdf* __restrict__ wnew = dp ? dp->wnew : wnew_a;
+    const qdf* __restrict__ w1 = dp ? dp->w1 : w1_a;
+    const qdf* __restrict__ w2 = dp ? dp->w2 : w2_a;
+    const double* __restrict__ hx = dp ? dp->hx : R.hx;
     const double* __restrict__ sg = R.sg;
     float racc = 0.f, xacc = 0.f;
     for (unsigned base = blockIdx.x * 64u; base < Nn; base += gridDim.x * 64u) {
@@ -729,7 +739,8 @@ void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const
 }
 
 void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
-                           const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st) {
+                           const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st,
+                           const QStepPtrs* dptrs) {
     QStartRhs R{};
     if (h.hx) {
         R.hx = h.hx;
@@ -741,7 +752,7 @@ void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const dou
         R.x0 = h.x0;
     }
     qk_step_start<<<(unsigned)nb, 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3, h.xo, h.wnew,
-                                                 h.w1, h.w2, rfloat, partials, R);
+                                                 h.w1, h.w2, rfloat, partials, R, dptrs);
 }
 
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st) {

@@ -53,9 +53,23 @@ struct QStepStart {
     double dt;
     double* x0;
 };
+// the history pointers that rotate from step to step, for a step start that reads them from
+// device memory (dptrs) instead of its arguments (with hx: the pointers are those of h)
+struct QStepPtrs {
+    const double* xo1;
+    const double* xo2;
+    const double* xo3;
+    qdf* wnew;
+    const qdf* w1;
+    const qdf* w2;
+    const double* hx;
+    const double* b;
+    const double* bprev;
+};
 // nb: the blocks of the launch and the partials per quantity
 void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
-                           const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st);
+                           const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st,
+                           const QStepPtrs* dptrs = nullptr);
 // 1 / diag M as double-float (padded layout)
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st);
 // dx = x - x0 as double-float (padded layout) and the partials |x_A|^2, |x_V|^2 of nb blocks

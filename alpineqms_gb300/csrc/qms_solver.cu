@@ -33,6 +33,8 @@ enum {
     S_RR0, S_RR,                  // inner residual norms^2 (initial, current)
     S_RHO, S_ALPHA, S_OMEGA, S_BETA,
     S_RZ, S_RZ0,
+    // the convergence test of a step captured whole (qk_cond_init / qk_cond_next)
+    S_SREF = 23, S_REL, S_REL0, S_CYC, S_PRN, S_PRN_LAST,
     S_COUNT = 32
 };
 
@@ -101,6 +103,40 @@ __global__ void qk_finalize(const double* __restrict__ part, long long nb, int n
         break;
     }
     }
+}
+
+// --------------------------------------------------------------------------
+// convergence test of a whole step captured in one graph: the host loop's relative residual
+// rel = |r| / min(max(|x|, s), 100 s), s = |x| at the start of the solve, from the finalized
+// residual sums; the WHILE node runs another refinement cycle while rel > tol, at most
+// maxcyc cycles, and while each cycle at least removes a tenth of the residual
+// --------------------------------------------------------------------------
+__global__ void qk_cond_init(double* __restrict__ S, double tol, cudaGraphConditionalHandle hc) {
+    if (threadIdx.x != 0) return;
+    const double xn = sqrt(S[S_XA] + S[S_XV]), rn = S[S_NRM];
+    const double sref = xn > 0.0 ? xn : 1.0;
+    const double rel = rn / fmin(fmax(xn, sref), 100.0 * sref);
+    S[S_SREF] = sref;
+    S[S_REL] = rel;
+    S[S_REL0] = rel;
+    S[S_CYC] = 0.0;
+    S[S_PRN] = rn;
+    S[S_PRN_LAST] = rn;
+    cudaGraphSetConditional(hc, (isfinite(rel) && rel > tol && rn != 0.0) ? 1u : 0u);
+}
+
+__global__ void qk_cond_next(double* __restrict__ S, double tol, int maxcyc, cudaGraphConditionalHandle hc) {
+    if (threadIdx.x != 0) return;
+    const double xn = sqrt(S[S_XA] + S[S_XV]), rn = S[S_NRM], sref = S[S_SREF];
+    const double rel = rn / fmin(fmax(xn, sref), 100.0 * sref);
+    const double prev = S[S_PRN];
+    const double cyc = S[S_CYC] + 1.0;
+    S[S_CYC] = cyc;
+    S[S_REL] = rel;
+    S[S_PRN_LAST] = prev;
+    S[S_PRN] = rn;
+    const bool more = isfinite(rel) && rel > tol && rn != 0.0 && cyc < (double)maxcyc && rn < 0.9 * prev;
+    cudaGraphSetConditional(hc, more ? 1u : 0u);
 }
 
 // --------------------------------------------------------------------------
@@ -512,6 +548,10 @@ void QmsSolver::release() {
                     rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2, hist_x, xold3, wh[0], wh[1], wh[2]};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
+    if (hptrs) cudaFreeHost(hptrs);
+    if (dptrs) cudaFree(dptrs);
+    hptrs = nullptr;
+    dptrs = nullptr;
     for (auto& p : vec) if (p) cudaFree(p);
     drop_graphs();
     for (auto& e : evpool) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
@@ -629,6 +669,8 @@ int QmsSolver::init(const qms_desc& d) {
         CK(pl_alloc((void**)&dinvdf, 8));
         CK(cudaMalloc(&x0, n * 8));
         CK(pl_alloc((void**)&rpl, 4));
+        CK(cudaMallocHost(&hptrs, sizeof(QStepPtrs)));
+        CK(cudaMalloc(&dptrs, sizeof(QStepPtrs)));
         CK(cudaMalloc(&ncdf, 6 * qms_pl(g).comp * 8));
         CK(cudaMemsetAsync(ncdf, 0, 6 * qms_pl(g).comp * 8, st));
         if (!qms_make_pl_map(&xdfmap, xdf, g, 8, 4, PLXY) || !qms_make_pl_map(&cdfmap, ncdf, g, 8, 6, PLCY)) {
@@ -1134,6 +1176,107 @@ void QmsSolver::drop_graphs() {
         for (auto& e : G.ev) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     }
     graphs.clear();
+    for (StepGraph& G : sgraphs)
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+    sgraphs.clear();
+}
+
+// One whole chained step as a graph (captured once per k, start variant and velocity, then
+// replayed): returns after the step with the residual sums in hS and the cycles it ran.
+int QmsSolver::step_graph(bool adv, const double v[3], const QStepStart& hs, bool wcalc, int k, int& cycles) {
+    const bool dbx = hs.hx != nullptr;
+    StepGraph* G = nullptr;
+    for (StepGraph& e : sgraphs)
+        if (e.k == k && e.xo == hs.xo && e.wcalc == wcalc && e.dbx == dbx && e.v[0] == v[0] && e.v[1] == v[1] &&
+            e.v[2] == v[2]) { G = &e; break; }
+    if (!G) {
+        constexpr size_t kMax = 4;
+        if (sgraphs.size() >= kMax) {
+            size_t lru = 0;
+            for (size_t q = 1; q < sgraphs.size(); q++) if (sgraphs[q].used < sgraphs[lru].used) lru = q;
+            if (sgraphs[lru].exec) cudaGraphExecDestroy(sgraphs[lru].exec);
+            sgraphs.erase(sgraphs.begin() + (long)lru);
+        }
+        StepGraph ng;
+        cudaGraph_t graph = nullptr;
+        CK(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle hc;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&hc, graph, 0, cudaGraphCondAssignDefault);
+        const long long n0 = nlaunch;
+        int rc = 0;
+        if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            capturing = true;
+            cudaMemsetAsync(status, 0, 4, st);
+            cudaMemcpyAsync(dptrs, hptrs, sizeof(QStepPtrs), cudaMemcpyHostToDevice, st);
+            qms_launch_step_start(g, rfin, b, bprev, dinvdf, r0df, hs, rpl, part, nbop, st, dptrs);
+            finalize(FIN_RESID, 4, nbop);
+            qk_cond_init<<<1, 32, 0, st>>>(S, desc.tol, hc);
+            nlaunch += 2;
+            ng.pro = nlaunch - n0;
+            // the conditional node at the end of the prologue
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t cg = nullptr;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd);
+            cudaGraphNodeParams cp = {};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = hc;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t cn = nullptr;
+            if (e == cudaSuccess) e = cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &cp);
+            if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies);
+            cudaGraph_t got = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(st, &got);
+            if (e == cudaSuccess) e = e2;
+            // the body: one refinement cycle and the test that sets the condition
+            if (e == cudaSuccess) {
+                cudaGraph_t body = cp.conditional.phGraph_out[0];
+                e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    const long long n1 = nlaunch;
+                    int it = 0;
+                    start_resid_ready = false;          // the body's residual is the double-float one
+                    rc = inner_gmres<float>(adv, true, v, it, k);
+                    if (rc == 0) rc = residual_launch(adv, true, v);
+                    qk_cond_next<<<1, 32, 0, st>>>(S, desc.tol, kStepGraphCycles, hc);
+                    nlaunch++;
+                    ng.body = nlaunch - n1;
+                    cudaGraph_t bg = nullptr;
+                    e2 = cudaStreamEndCapture(st, &bg);
+                    if (e == cudaSuccess) e = e2;
+                }
+            }
+            capturing = false;
+        }
+        nlaunch = n0;
+        if (rc == 0 && e == cudaSuccess) e = cudaGraphInstantiate(&ng.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (rc || e != cudaSuccess) {
+            cudaGetLastError();
+            if (ng.exec) cudaGraphExecDestroy(ng.exec);
+            if (rc) return rc;
+            err = std::string("step graph: ") + cudaGetErrorString(e);
+            return QMS_ERR_CUDA;
+        }
+        ng.k = k; ng.xo = hs.xo; ng.wcalc = wcalc; ng.dbx = dbx;
+        ng.v[0] = v[0]; ng.v[1] = v[1]; ng.v[2] = v[2];
+        sgraphs.push_back(ng);
+        G = &sgraphs.back();
+    }
+    // the rotating pointers of this step, read by the graph's copy node at launch
+    *hptrs = QStepPtrs{hs.xo1, hs.xo2, hs.xo3, hs.wnew, hs.w1, hs.w2, hs.hx, b, bprev};
+    G->used = ++graph_clock;
+    CK(cudaGraphLaunch(G->exec, st));
+    int rc = read_scalars();                    // synchronises the stream
+    if (rc) return rc;
+    cycles = (int)hS[S_CYC];
+    nlaunch += G->pro + (long long)cycles * G->body;
+    last_resid_df = true;
+    start_resid_ready = false;
+    return 0;
 }
 
 int QmsSolver::ir_iteration_graph(bool adv, bool transient, const double v[3], int k) {
@@ -1235,6 +1378,13 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // (the step start, in double-float) and this solve forms no FP64 right-hand side
     const bool db_from_x = chain && same_field && hist_len >= 2 && hist_x && xold && rsg;
     start_resid_ready = false;
+    // the whole step as one graph: a chained step whose start also forms the first residual, with
+    // replayed refinement cycles of a known count (no profile events inside: they cannot live in
+    // a conditional body)
+    const bool use_step_graph = desc.use_graphs && desc.krylov == QMS_KRYLOV_GMRES && start_fused && db_from_x &&
+                                gm_k_est > 0 && !prof && !trace && hptrs;
+    QStepStart sg_hs{};
+    bool sg_wcalc = false;
     if (chain && !db_from_x) {
         ensure_b();                // b_prev: the last solve's right-hand side
         // x0 is copied, not swapped: the captured refinement graphs hold its address
@@ -1259,10 +1409,15 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         const int nw = std::min(desc.extrapolate, 3);          // w buffers: w_(n-1), w_(n-2), the new one
         QStepStart hs{x,       xold, xold2, xold3, xo, wcalc ? wh[nw - 1] : nullptr, wh[0], wh[1],
                       db_from_x ? hist_x : nullptr, rsg, rsdt, desc.dt, db_from_x ? x0 : nullptr};
-        OpEv* ev = start_fused ? prof_begin(3, (double)g.n * (8 * 11 + 8 * 2 * xo + 4)) : nullptr;
-        qms_launch_step_start(g, rfin, b, bprev, dinvdf, r0df, hs, start_fused ? rpl : nullptr, part, nbop, st);
-        nlaunch++;
-        prof_end(ev);
+        if (use_step_graph) {
+            sg_hs = hs;                  // launched inside the step's graph below
+            sg_wcalc = wcalc;
+        } else {
+            OpEv* ev = start_fused ? prof_begin(3, (double)g.n * (8 * 11 + 8 * 2 * xo + 4)) : nullptr;
+            qms_launch_step_start(g, rfin, b, bprev, dinvdf, r0df, hs, start_fused ? rpl : nullptr, part, nbop, st);
+            nlaunch++;
+            prof_end(ev);
+        }
         if (wcalc) {               // wh[0]: w_n, wh[1]: w_(n-1), the oldest becomes the next one's buffer
             qdf* fresh = wh[nw - 1];
             for (int q = nw - 1; q > 0; q--) wh[q] = wh[q - 1];
@@ -1286,7 +1441,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     }
     last_chained = chain;
     rfin_ok = false;
-    CK(cudaMemsetAsync(status, 0, 4, st));
+    if (!use_step_graph) CK(cudaMemsetAsync(status, 0, 4, st));
     const bool adv = v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
     const bool use_cg = !transient && !adv;
     stats = qms_stats{};
@@ -1299,6 +1454,25 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     int gm_cycles = 0;                    // FGMRES cycles run in this solve
     int graph_cycles = 0;                 // ... of them replayed from graphs
     double best_rn = INFINITY, best_rel = INFINITY;
+    if (use_step_graph) {
+        // the step (start and up to kStepGraphCycles cycles) in one graph; the loop below takes
+        // over from the residual it leaves, as after a replayed cycle
+        int cyc = 0;
+        int rc = step_graph(adv, v, sg_hs, sg_wcalc, gm_k_est, cyc);
+        if (rc) return rc;
+        graph_resid_ready = true;
+        stats.initial_residual = hS[S_REL0];
+        if (cyc > 0) {
+            outer = cyc;
+            sref = hS[S_SREF];
+            prev_rn = hS[S_PRN_LAST];
+            gm_k_last = graph_k_used = gm_k_est;
+            gm_cycles = graph_cycles = cyc;
+            stats.inner_iterations = cyc * gm_k_est;
+            last_inner = 2;
+            last_gm_k = gm_k_est;
+        }
+    }
     for (;;) {
         int rc = 0;
         if (!graph_resid_ready) {

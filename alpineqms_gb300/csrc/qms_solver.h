@@ -5,6 +5,7 @@
 #include "qms_mg.h"
 #include "qms_tma.cuh"
 #include "qms_df.cuh"
+#include "qms_pl.h"
 
 #include <cuda_bf16.h>
 
@@ -198,6 +199,25 @@ struct QmsSolver {
         unsigned long long used = 0;
     };
     std::vector<IrGraph> graphs;
+    // Whole chained transient steps as one CUDA graph each: the status reset, the step start (its
+    // rotating history pointers copied from pinned host memory by a node of the graph), the start
+    // residual, and a conditional WHILE node whose body is one refinement cycle (FGMRES with k
+    // steps, the FP64 update, the double-float residual) ended by a kernel that sets the
+    // condition from the residual (at most kStepGraphCycles cycles; the host loop continues a
+    // solve that needs more).  One host synchronisation per step.
+    static constexpr int kStepGraphCycles = 3;
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        int k = 0, xo = 0;
+        bool wcalc = false, dbx = false;
+        double v[3] = {0, 0, 0};
+        long long pro = 0, body = 0;     // kernel launches of the prologue and of one cycle
+        unsigned long long used = 0;
+    };
+    std::vector<StepGraph> sgraphs;
+    QStepPtrs* hptrs = nullptr;          // pinned host copy of the step start's rotating pointers
+    QStepPtrs* dptrs = nullptr;          // ... and the device copy the graph's step start reads
+    int step_graph(bool adv, const double v[3], const QStepStart& hs, bool wcalc, int k, int& cycles);
     unsigned long long graph_clock = 0;
     void drop_graphs();
     bool graph_resid_ready = false;
