@@ -50,7 +50,7 @@ class QmsStats(ctypes.Structure):
                 ("inner_iterations", ctypes.c_int),
                 ("initial_residual", ctypes.c_double),
                 ("final_residual", ctypes.c_double),
-                ("status", ctypes.c_uint)]
+                ("status", ctypes.c_uint), ("step_graph", ctypes.c_int)]
 
 
 class QmsProfile(ctypes.Structure):

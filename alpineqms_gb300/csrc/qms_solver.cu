@@ -1461,6 +1461,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         int rc = step_graph(adv, v, sg_hs, sg_wcalc, gm_k_est, cyc);
         if (rc) return rc;
         graph_resid_ready = true;
+        stats.step_graph = 1;
         stats.initial_residual = hS[S_REL0];
         if (cyc > 0) {
             outer = cyc;

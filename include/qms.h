@@ -132,6 +132,8 @@ typedef struct {
     double initial_residual; /* relative scaled residual before the solve */
     double final_residual;   /* after */
     unsigned status;         /* QMS_STATUS_* bits */
+    int step_graph;          /* 1 when the step ran as one CUDA graph (start, residual and its refinement
+                                cycles behind a device-side convergence test), 0 otherwise */
 } qms_stats;
 
 typedef struct qms_handle qms_handle;
