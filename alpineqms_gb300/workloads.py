@@ -123,13 +123,13 @@ def serving_request(rng, sizes=SERVING_SIZES, nt=50, h=1e-3):
     return inp, geom.flatten(order="F")
 
 
-def laminated_core(nt=100, shape=(512, 512, 256), h=0.25e-3):
+def laminated_core(nt=100, shape=(512, 512, 256), h=0.25e-3, laminations=40):
     xs, ys, zs = shape
     geom = np.zeros(shape)
-    stack = 40 * 5 + 39
+    stack = laminations * 5 + laminations - 1
     z0 = (zs - stack) // 2
     mx, my = xs // 8, ys // 8
-    for L in range(40):
+    for L in range(laminations):
         z = z0 + L * 6
         geom[mx:xs - mx, my:ys - my, z:z + 5] = 1
     inp = _inputs(shape, h, 1.6e-4, nt, (0.5, 0.0, 0.0), np.zeros(9), [(0.0, 0.0, 0)] * 3,

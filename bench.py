@@ -313,7 +313,9 @@ def run_gpu(args):
     if dist:
         dist.barrier()
     clocks.start()
+    torch.cuda.nvtx.range_push("timed_steps")     # lets a profiler capture exactly these steps
     ms_local, iters = timed_steps(run, K, ext)
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     ms, units = aggregate_replicas(ms_local, n * K, dist, "cuda")
     if dist:
