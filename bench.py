@@ -58,6 +58,9 @@ def parse_args():
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the plain FP64 GPU solver leg (its timing and the per-step comparison)")
     ap.add_argument("--workload", default="moving_plate_256", choices=WORKLOADS)
+    ap.add_argument("--serving-requests", type=int, default=24,
+                    help="requests of the serving sample reported beside the line (0: none)")
+    ap.add_argument("--serving-steps", type=int, default=10)
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="steps of the kernel-timing pass (0: as many as the timed steps)")
     ap.add_argument("--fp64-steps", type=int, default=0,
@@ -462,6 +465,27 @@ def run_gpu(args):
         roofline["inner_stencil_fp32"] = {"launches": prof["op32_launches"],
                                           "achieved_gbs": prof["op32_bytes"] / (prof["op32_ms"] / 1e3) / 1e9}
 
+    # -- 5. the serving half of the metric: a sample of the seeded request stream (the first
+    # requests of the 512-request stream, fewer steps each) through the native serving object,
+    # with its per-step and per-request latency percentiles
+    serving = None
+    if rank == 0 and args.serving_requests > 0 and args.precision == "mixed":
+        from alpineqms_gb300 import serving as srv_mod
+        reqs, gaps = srv_mod.poisson_stream(args.serving_requests, 0.05, nt=args.serving_steps)
+        t0 = time.perf_counter()
+        with srv_mod.NativeServer(150 << 30, 16, device=local) as srv:
+            res = srv.serve(reqs, gaps)
+            wall = time.perf_counter() - t0
+            rep = srv_mod.latency_report(res, wall)
+            st_ = srv.stats()
+        serving = {"sample": "the first %d requests of the seeded 512-request stream (48^3..128^3, 8-32 "
+                             "random ellipsoids, Poisson arrivals 50 ms mean gap), %d steps each, 16 resident, "
+                             "150 GB budget" % (args.serving_requests, args.serving_steps),
+                   "completed": rep["completed"], "failed": rep["failed"],
+                   "step_p50_ms": st_["step_p50_ms"], "step_p99_ms": st_["step_p99_ms"],
+                   "request_p50_s": rep["request_p50_s"], "request_p99_s": rep["request_p99_s"],
+                   "dof_timesteps_per_s": rep["dof_timesteps_per_s"], "wall_s": wall}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -488,7 +512,7 @@ def run_gpu(args):
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                            "l2": "inputs larger than L2 (one FP32 vector = %.0f MB)" % (n * 4 / 1e6)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": prof["launches"],
-                "fp64": fp64, "accuracy": accuracy,
+                "fp64": fp64, "accuracy": accuracy, "serving": serving,
                 "clocks": clk, "steady_s": steady_s,
                 "steady_iters": {"outer": st0["outer"], "inner": st0["inner"]},
                 "step_iters": [{"outer": q["outer"], "inner": q["inner"], "r0": q["r0"], "r": q["r"]}
