@@ -42,7 +42,8 @@ class QmsDesc(ctypes.Structure):
                 ("mg_alpha", ctypes.c_double), ("mg_coupling", ctypes.c_int),
                 ("mg_coarse_sweeps", ctypes.c_int), ("mg_v_sweeps", ctypes.c_int),
                 ("mg_tail_points", ctypes.c_int), ("extrapolate", ctypes.c_int),
-                ("mg_v_coarse_cut", ctypes.c_double), ("gm_first_extend", ctypes.c_int)]
+                ("mg_v_coarse_cut", ctypes.c_double), ("gm_first_extend", ctypes.c_int),
+                ("tol_v", ctypes.c_double)]
 
 
 class QmsStats(ctypes.Structure):

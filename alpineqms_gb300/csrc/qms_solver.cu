@@ -1382,7 +1382,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // replayed refinement cycles of a known count (no profile events inside: they cannot live in
     // a conditional body)
     const bool use_step_graph = desc.use_graphs && desc.krylov == QMS_KRYLOV_GMRES && start_fused && db_from_x &&
-                                gm_k_est > 0 && !prof && !trace && hptrs;
+                                gm_k_est > 0 && !prof && !trace && hptrs && !(desc.tol_v > 0.0);
     QStepStart sg_hs{};
     bool sg_wcalc = false;
     if (chain && !db_from_x) {
@@ -1491,7 +1491,11 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         rel = rn / scale;
         if (outer == 0) stats.initial_residual = rel;
         if (!std::isfinite(rel)) { stats.status |= QMS_ST_NAN; break; }
-        if (rel <= desc.tol || rn == 0.0) break;
+        // optionally the potential block on its own scale as well: where |x| is dominated by A
+        // (slow fields, small potentials), rel alone does not bound V's relative error
+        const bool v_ok = !(desc.tol_v > 0.0) || hS[S_XV] == 0.0 ||
+                          std::sqrt(hS[S_RV]) <= desc.tol_v * std::sqrt(hS[S_XV]);
+        if ((rel <= desc.tol && v_ok) || rn == 0.0) break;
         // Per-step reduction rate of FGMRES from the true residuals around each cycle, kept
         // apart for the first cycle of a solve and the later ones and smoothed in log space;
         // it sizes the next replay.  A replay that gained less than a tenth per cycle while k

@@ -124,6 +124,8 @@ typedef struct {
                                 and the observed first-cycle rate say that one cycle then reaches the
                                 tolerance (instead of two cycles); 0 = never (the default: on the
                                 moving plate it kept longer single cycles, 30.6 vs 28.0 ms per step) */
+    double tol_v;            /* > 0: a solve also stops only when ||r_V|| <= tol_v * ||x_V|| (the potential block's
+                                scaled residual against its own size); 0 = off (the default) */
 } qms_desc;
 
 typedef struct {
