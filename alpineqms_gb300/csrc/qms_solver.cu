@@ -254,7 +254,10 @@ __global__ void qk_cg_p(long long n, const T* __restrict__ z, T* __restrict__ p,
 // FGMRES (right preconditioned, restarted by the outer refinement) with the
 // Hessenberg matrix, Givens rotations and the residual estimate on the device.
 // --------------------------------------------------------------------------
-#define GM_MAXM 32
+// basis of up to 64 vectors; the Gram-Schmidt and update kernels take at most GM_PASS of them
+// per launch (compile-time counts), so longer bases run as two passes
+#define GM_MAXM 64
+#define GM_PASS 32
 struct GmPtrs { const void* p[GM_MAXM + 1]; };
 
 // block partials of V_i . w for i = 0..NV-1 (classical Gram-Schmidt projections).
@@ -340,16 +343,17 @@ __global__ void qk_gm_hcol(const double* __restrict__ part, long long nb, int j,
 // w' = w - sum_i h_ij V_i (NV = j + 1, compile-time; 16-byte packets): with Gm[3] set, V_{j+1} =
 // w' / Gm[4] goes to vout; otherwise w' back into w with the partials of |w'|^2
 template <typename T, int NV>
+// final = 0: a first pass over part of the basis (w' back into w, no norm partials, no direct write)
 __global__ void __launch_bounds__(256) qk_gm_orth(long long n, int j, int m, GmPtrs V, const double* __restrict__ Hm,
                                                   T* __restrict__ w, double* __restrict__ part,
-                                                  const double* __restrict__ Gm, T* __restrict__ vout) {
+                                                  const double* __restrict__ Gm, T* __restrict__ vout, int final) {
     using PK = GmPack<T>;
     using PV = typename PK::V;
     T h[NV];
     const PV* vp[NV];
 #pragma unroll
     for (int i = 0; i < NV; i++) { h[i] = (T)Hm[i * m + j]; vp[i] = (const PV*)V.p[i]; }
-    const bool direct = Gm[3] != 0.0;
+    const bool direct = final && Gm[3] != 0.0;
     const T inv = direct ? (T)(1.0 / Gm[4]) : T(1);
     PV* wp = (PV*)w;
     PV* op = direct ? (PV*)vout : wp;
@@ -371,7 +375,7 @@ __global__ void __launch_bounds__(256) qk_gm_orth(long long n, int j, int m, GmP
         }
         op[t] = wv;
     }
-    if (direct) return;
+    if (direct || !final) return;
     __shared__ double sh[32];
     double s0 = qBlockSum(acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = s0;
@@ -470,31 +474,56 @@ __global__ void __launch_bounds__(QMS_NODE_BX * QMS_NODE_BY) qk_gm_update(QGrid 
 #define GM_CASES(M) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11) M(12) M(13) M(14) M(15) M(16) \
     M(17) M(18) M(19) M(20) M(21) M(22) M(23) M(24) M(25) M(26) M(27) M(28) M(29) M(30) M(31) M(32)
 
+static GmPtrs gm_shift(const GmPtrs& V, int off) {
+    GmPtrs r{};
+    for (int i = 0; i + off <= GM_MAXM; i++) r.p[i] = V.p[i + off];
+    return r;
+}
+// returns the kernel launches
 template <typename T>
-static void gm_dots(int nv, int vb, cudaStream_t st, long long n, const GmPtrs& V, const T* w, double* part) {
+static int gm_dots(int nv, int vb, cudaStream_t st, long long n, const GmPtrs& V, const T* w, double* part) {
+    if (nv > GM_PASS) {
+        // the first GM_PASS projections, then the rest (whose |w|^2 partials land at nv * vb)
+        gm_dots<T>(GM_PASS, vb, st, n, V, w, part);
+        return 1 + gm_dots<T>(nv - GM_PASS, vb, st, n, gm_shift(V, GM_PASS), w, part + (long long)GM_PASS * vb);
+    }
     switch (nv) {
 #define C(N) case N: qk_gm_dots<T, N><<<vb, 256, 0, st>>>(n, V, w, part); break;
         GM_CASES(C)
 #undef C
     }
+    return 1;
 }
 template <typename T>
-static void gm_orth(int nv, int vb, cudaStream_t st, long long n, int j, int m, const GmPtrs& V, const double* Hm, T* w,
-                    double* part, const double* Gm, T* vout) {
+static int gm_orth(int nv, int vb, cudaStream_t st, long long n, int j, int m, const GmPtrs& V, const double* Hm, T* w,
+                   double* part, const double* Gm, T* vout, int final = 1) {
+    if (nv > GM_PASS) {
+        gm_orth<T>(GM_PASS, vb, st, n, j, m, V, Hm, w, part, Gm, vout, 0);
+        return 1 + gm_orth<T>(nv - GM_PASS, vb, st, n, j, m, gm_shift(V, GM_PASS), Hm + (long long)GM_PASS * m, w,
+                              part, Gm, vout, final);
+    }
     switch (nv) {
-#define C(N) case N: qk_gm_orth<T, N><<<vb, 256, 0, st>>>(n, j, m, V, Hm, w, part, Gm, vout); break;
+#define C(N) case N: qk_gm_orth<T, N><<<vb, 256, 0, st>>>(n, j, m, V, Hm, w, part, Gm, vout, final); break;
         GM_CASES(C)
 #undef C
     }
+    return 1;
 }
 template <typename T>
-static void gm_update(int nv, cudaStream_t st, const QGrid& g, int m, const GmPtrs& Z, const double* Gm,
-                      const double* S, double* x) {
+static int gm_update(int nv, cudaStream_t st, const QGrid& g, int m, const GmPtrs& Z, const double* Gm,
+                     const double* S, double* x) {
+    if (nv > GM_PASS) {
+        // x += nr (sum of the first GM_PASS terms) + nr (the rest): the y of the second pass start
+        // GM_PASS further into Gm
+        gm_update<T>(GM_PASS, st, g, m, Z, Gm, S, x);
+        return 1 + gm_update<T>(nv - GM_PASS, st, g, m, gm_shift(Z, GM_PASS), Gm + GM_PASS, S, x);
+    }
     switch (nv) {
 #define C(N) case N: qk_gm_update<T, N><<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, m, Z, Gm, S, x); break;
         GM_CASES(C)
 #undef C
     }
+    return 1;
 }
 
 
@@ -1033,12 +1062,12 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
         T* zj = use_mg ? (T*)gmZ[j] : vj;
         if (use_mg) precond<T>(vj, dg, zj, false, transient, false, &P, adv);
         op_pl<T>(adv, QOPH_SCALED, P, zj, w, nullptr, nullptr);
-        gm_dots<T>(j + 1, vb, st, n, Vp, w, part);
+        nlaunch += gm_dots<T>(j + 1, vb, st, n, Vp, w, part);
         qk_gm_hcol<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H, gm_scal);
-        gm_orth<T>(j + 1, vb, st, n, j, m, Vp, gm_H, w, part, gm_scal, (T*)gmV[j + 1]);
+        nlaunch += gm_orth<T>(j + 1, vb, st, n, j, m, Vp, gm_H, w, part, gm_scal, (T*)gmV[j + 1]);
         qk_gm_givens<<<1, 512, 0, st>>>(part, vec_blocks, j, m, gm_H, gm_scal, status);
         qk_gm_scale<T><<<vb, 256, 0, st>>>(n, w, (T*)gmV[j + 1], gm_scal);
-        nlaunch += 5;
+        nlaunch += 3;
         k = j + 1;
         if (fixed_k <= 0 && ((j + 1) % desc.check_every == 0 || j + 1 == m)) {
             CK(cudaMemcpyAsync(hS, gm_scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1047,8 +1076,7 @@ int QmsSolver::inner_gmres(bool adv, bool transient, const double v[3], int& ite
         }
     }
     qk_gm_solve<<<1, 32, 0, st>>>(k, m, gm_H, gm_scal);
-    gm_update<T>(k, st, g, m, Zp, gm_scal, S, x);
-    nlaunch += 2;
+    nlaunch += 1 + gm_update<T>(k, st, g, m, Zp, gm_scal, S, x);
     last_gm_k = k;
     iters = k;
     CK(cudaGetLastError());

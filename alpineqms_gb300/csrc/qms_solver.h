@@ -229,8 +229,8 @@ struct QmsSolver {
     // log of the per-iteration residual reduction of FGMRES, smoothed over solves: [0] the first
     // cycle of a solve, [1] the later ones (which start from a residual rich in slow modes)
     double gm_lrate[2] = {0, 0};
-    void* gmV[33] = {};         // FGMRES basis (m + 1) and preconditioned directions (m)
-    void* gmZ[32] = {};
+    void* gmV[65] = {};         // FGMRES basis (m + 1) and preconditioned directions (m), m <= 64
+    void* gmZ[64] = {};
     double* gm_H = nullptr;     // Hessenberg matrix (m+1) x m, row-major with stride m
     double* gm_scal = nullptr;  // beta, |g_{j+1}|, 1/h, rotations, g, y
     int last_gm_k = 0;

@@ -90,7 +90,7 @@ typedef struct {
                                 the coarsest V solve is a pseudo-inverse that drops the floating
                                 potential of isolated conductors) */
     int krylov;              /* nonsymmetric inner solver: QMS_KRYLOV_GMRES (default) or _BICGSTAB */
-    int gmres_m;             /* FGMRES basis size per refinement iteration (<= 32) */
+    int gmres_m;             /* FGMRES basis size per refinement iteration (<= 64) */
     int use_graphs;          /* replay each refinement iteration of a step as one CUDA graph, with the
                                 FGMRES iteration count learned from the first solve (1 = on) */
     double mg_region_cut;    /* conductor-region coarse space of the potential block: eigenvalues of

@@ -1,4 +1,4 @@
-"""Whole time steps captured as one CUDA graph.
+"""Whole time steps captured as one CUDA graph, and FGMRES bases longer than one kernel pass.
 
 A chained transient step (same operator as the step before, the field unchanged, the start
 residual formed by the step start) runs as one graph: the status reset, the step start with
@@ -58,3 +58,33 @@ def test_chained_steps_run_as_one_graph_and_match_fp64():
     assert graphs >= inp.nt - 8, graphs
     s.close()
     r64.close()
+
+
+def test_long_fgmres_basis_two_passes():
+    """FGMRES cycles longer than 32 steps run their Gram-Schmidt and update kernels in two
+    passes over the basis; a 48-step basis forced to full length (inner_rtol 1e-30, no graphs)
+    reaches the tolerance and agrees with the 32-step solver within 1e-8."""
+    from alpineqms_gb300 import workloads
+    from alpineqms_gb300.solver import QMSSolver, default_desc
+    from alpineqms_gb300.trajectory import VelocitySchedule, scaled_field
+    from alpineqms_gb300 import serving
+    reqs, _ = serving.poisson_stream(5, 0.05, nt=50)
+    inp, geom = reqs[4].inputs, reqs[4].geom           # 48^3, 22 random ellipsoids
+    out = {}
+    for name, kw in (("m32", {}), ("m48", dict(gmres_m=48, inner_rtol=1e-30, use_graphs=0))):
+        s = QMSSolver(default_desc(inp.xs, inp.ys, inp.zs, inp.dx, inp.dy, inp.dz, inp.dt, **kw))
+        s.set_geometry_f64(geom, inp.props_table())
+        sched = VelocitySchedule(inp.traj, inp.dt)
+        B, G = scaled_field(inp.B, inp.G, inp.excitation, 0.0)
+        s.steady(sched.steady(), B, G)
+        for k in (1, 2):
+            B, G = scaled_field(inp.B, inp.G, inp.excitation, k * inp.dt)
+            st = s.step(sched.step(k), B, G)
+            assert st["status"] == 0 and st["r"] <= 2e-13, (name, k, st)
+        if name == "m48":
+            assert st["inner"] >= 48 * st["outer"] - 1, st     # the cycles ran past 32 steps
+        out[name] = s.get_state()
+        s.close()
+    oV = out["m32"].size - (inp.xs + 1) * (inp.ys + 1) * (inp.zs + 1)
+    a, b = out["m48"][:oV], out["m32"][:oV]
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 1e-8
