@@ -74,7 +74,8 @@ class QmsRequest(ctypes.Structure):
                 ("slice_index", ctypes.c_int), ("keep", ctypes.c_int), ("precision", ctypes.c_int),
                 ("B", ctypes.c_double * 3), ("G", ctypes.c_double * 9), ("traj", (ctypes.c_double * 3) * 3),
                 ("exc_kind", ctypes.c_int), ("exc_f", ctypes.c_double), ("exc_phase", ctypes.c_double),
-                ("geom", ctypes.c_void_p), ("table", ctypes.c_void_p), ("nmat", ctypes.c_int)]
+                ("geom", ctypes.c_void_p), ("table", ctypes.c_void_p), ("nmat", ctypes.c_int),
+                ("traj_kind", ctypes.c_int * 3), ("traj_table", ctypes.c_void_p * 3), ("traj_len", ctypes.c_int * 3)]
 
 
 class QmsSrvResult(ctypes.Structure):
@@ -153,6 +154,7 @@ SIGNATURES = [
     ("qms_srv_error", ctypes.c_char_p, [_H, ctypes.c_longlong]),
     ("qms_srv_stats_get", ctypes.c_int, [_H, ctypes.POINTER(QmsSrvStats)]),
     ("qms_srv_destroy", None, [_H]),
+    ("qms_srv_velocities", ctypes.c_int, [ctypes.POINTER(QmsRequest), ctypes.c_int, _VP]),
 ]
 STRUCTS.update({"qms_desc": QmsDesc, "qms_stats": QmsStats, "qms_profile": QmsProfile})
 

@@ -43,40 +43,71 @@ double trajectory_1(double v0, double a, int nacc, int n, double dt) {
     return r;
 }
 
+// trajectory type 2 (harmonic motion, an extension: the reference stops on it, F:135-151)
+double trajectory_2(double amp, double f, double phase, int n, double dt) {
+    const double two_pi = 6.283185307179586;   // 2 * pi, rounded to double
+    return amp * std::sin(two_pi * f * (n * dt) + phase);
+}
+
 // The frame velocity of the steady state and of each step, with the pad of the first
 // step: when a dt < v0 * 1E-8 (a default-real literal) the first step accelerates by
-// v(0) * 1E-8 / dt (F:1428-1449); the pad state starts at zero (static storage).
+// v(0) * 1E-8 / dt (F:1428-1449); the pad state starts at zero (static storage).  The pad
+// belongs to type 1 (its test reads that type's a and v0); axes of type 2 (harmonic) and 3
+// (a per-step velocity table, the last entry held) get none.
 struct VelocitySchedule {
     double tr[3][3];
+    int kind[3];
+    const double* table[3];
+    int len[3];
     double dt;
     double v[3];
     double acc[3] = {0.0, 0.0, 0.0};
-    VelocitySchedule(const double t[3][3], double dt_) : dt(dt_) {
+    VelocitySchedule(const qms_request& r, const double* const tab[3]) : dt(r.dt) {
         for (int d = 0; d < 3; d++) {
-            for (int q = 0; q < 3; q++) tr[d][q] = t[d][q];
-            v[d] = trajectory_1(tr[d][0], tr[d][1], (int)tr[d][2], 0, dt);
+            for (int q = 0; q < 3; q++) tr[d][q] = r.traj[d][q];
+            kind[d] = r.traj_kind[d] == 0 ? 1 : r.traj_kind[d];
+            table[d] = tab[d];
+            len[d] = r.traj_len[d];
+            v[d] = velocity(d, 0, 0.0);
         }
+    }
+    double velocity(int d, int n, double pad) const {
+        if (kind[d] == 2) return trajectory_2(tr[d][0], tr[d][1], tr[d][2], n, dt);
+        if (kind[d] == 3) return table[d][n < len[d] - 1 ? n : len[d] - 1];
+        return trajectory_1(tr[d][0], tr[d][1] + pad, (int)tr[d][2], n, dt);
     }
     void step(int counter, double out[3]) {
         const double eps = (double)1e-8f;
         for (int d = 0; d < 3; d++) {
-            const double v0 = tr[d][0], a = tr[d][1];
-            const int nacc = (int)tr[d][2];
-            if (counter == 1) {
-                if (a * dt < v0 * eps) acc[d] = v[d] * eps / dt;
-            } else {
-                acc[d] = 0.0;
+            if (kind[d] == 1) {
+                const double v0 = tr[d][0], a = tr[d][1];
+                if (counter == 1) {
+                    if (a * dt < v0 * eps) acc[d] = v[d] * eps / dt;
+                } else {
+                    acc[d] = 0.0;
+                }
             }
-            out[d] = trajectory_1(v0, a + acc[d], nacc, counter, dt);
+            out[d] = velocity(d, counter, acc[d]);
         }
         for (int d = 0; d < 3; d++) v[d] = out[d];
     }
 };
 
+// Trajectory fields of a request: kinds 0 (= 1), 1, 2 or 3, a table of at least one value for 3.
+bool trajectory_ok(const qms_request& r) {
+    for (int d = 0; d < 3; d++) {
+        const int k = r.traj_kind[d];
+        if (k < 0 || k > 3) return false;
+        if (k == 3 && (!r.traj_table[d] || r.traj_len[d] < 1)) return false;
+    }
+    return true;
+}
+
 struct Request {
     long long id = 0;
     qms_request r{};                  // scalars; pointers cleared after the copy
     std::vector<double> geom, table;
+    std::vector<double> traj_table[3];    // velocity tables of type-3 axes
     size_t footprint = 0;
     int state = QMS_SRV_QUEUED;
     int rc = 0;
@@ -158,7 +189,8 @@ struct qms_server {
         if (rc == 0) {
             const int n1 = r.slice_axis == 0 ? r.ys : r.xs, n2 = r.slice_axis == 2 ? r.ys : r.zs;
             const size_t rec = 3 * (size_t)n1 * n2;
-            VelocitySchedule vs(r.traj, r.dt);
+            const double* tabs[3] = {q->traj_table[0].data(), q->traj_table[1].data(), q->traj_table[2].data()};
+            VelocitySchedule vs(r, tabs);
             auto field = [&](int n, double B[3], double G[9]) {
                 const double two_pi = 6.283185307179586;   // 2 * pi, rounded to double
                 double s = 1.0;
@@ -217,7 +249,7 @@ int qms_srv_create(const qms_srv_desc* d, qms_server** out) {
 int qms_srv_submit(qms_server* s, const qms_request* r, long long* id) {
     if (!s || !r || !id || !r->geom || (r->nmat > 0 && !r->table) || r->nmat < 0 || r->nt < 0) return QMS_ERR_ARG;
     if (r->xs < 4 || r->ys < 4 || r->zs < 4 || r->slice_axis < 0 || r->slice_axis > 2 || r->slice_index < 1 ||
-        r->slice_index > (r->slice_axis == 0 ? r->xs : r->slice_axis == 1 ? r->ys : r->zs))
+        r->slice_index > (r->slice_axis == 0 ? r->xs : r->slice_axis == 1 ? r->ys : r->zs) || !trajectory_ok(*r))
         return QMS_ERR_ARG;
     std::unique_ptr<Request> q(new (std::nothrow) Request());
     if (!q) return QMS_ERR_NOMEM;
@@ -226,6 +258,10 @@ int qms_srv_submit(qms_server* s, const qms_request* r, long long* id) {
     q->table.assign(r->table, r->table + 7 * (size_t)r->nmat);
     q->r.geom = nullptr;
     q->r.table = nullptr;
+    for (int d = 0; d < 3; d++) {
+        if (r->traj_kind[d] == 3) q->traj_table[d].assign(r->traj_table[d], r->traj_table[d] + r->traj_len[d]);
+        q->r.traj_table[d] = nullptr;
+    }
     qms_desc dd;
     qms_default_desc(&dd, r->xs, r->ys, r->zs, r->dx, r->dy, r->dz, r->dt);
     dd.precision = r->precision;
@@ -346,6 +382,15 @@ void qms_srv_destroy(qms_server* s) {
     s->admitter.join();                         // returns once every queued request was admitted
     for (auto& t : s->workers) t.join();
     delete s;
+}
+
+int qms_srv_velocities(const qms_request* r, int nsteps, double* out) {
+    if (!r || !out || nsteps < 0 || !trajectory_ok(*r)) return QMS_ERR_ARG;
+    const double* tabs[3] = {r->traj_table[0], r->traj_table[1], r->traj_table[2]};
+    VelocitySchedule vs(*r, tabs);
+    for (int d = 0; d < 3; d++) out[d] = vs.v[d];
+    for (int n = 1; n <= nsteps; n++) vs.step(n, out + 3 * (size_t)n);
+    return 0;
 }
 
 }  // extern "C"

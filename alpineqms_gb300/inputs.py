@@ -17,7 +17,17 @@ optional trailing line ``excitation,<cos|sin>,<f_Hz>[,<phase_rad>]`` scales
 the whole background field B_in + G.r by s(t) = cos(2 pi f t + phase) (or sin)
 at t = n*dt for step n (t = 0 for the steady state).
 
-Errors the reference reports with STOP (unsupported trajectory type,
+Extension (trajectory types the reference rejects with STOP, F:135-151; a file
+using them is therefore not one the reference runs): per axis, after the type
+line,
+
+* type 2, harmonic motion: one record ``amplitude, f_Hz, phase_rad``, the frame
+  velocity being v(n) = amplitude * sin(2 pi f n dt + phase);
+* type 3, a velocity table: a record ``n_points`` and then a record of that
+  many velocities (which may continue over several lines), v(n) = table[min(n,
+  n_points - 1)] for the steady state (n = 0) and each step n.
+
+Errors the reference reports with STOP (any other trajectory type,
 F:135-151) raise ``InputError`` with the same message.  Inputs on which the
 reference has undefined behaviour (slice axis not x/y/z, slice index out of
 range, tt <= 0, geometry IDs above the largest table ID or negative, no
@@ -48,10 +58,16 @@ class Material:
 
 @dataclasses.dataclass
 class Trajectory:
+    """One axis of the frame motion.  Type 1 (the reference's, F:136-137) uses v0, accel and
+    n_accel; type 2 (harmonic) amp, freq and phase; type 3 (velocity table) table."""
     kind: int
-    v0: float
-    accel: float
-    n_accel: int
+    v0: float = 0.0
+    accel: float = 0.0
+    n_accel: int = 0
+    amp: float = 0.0
+    freq: float = 0.0
+    phase: float = 0.0
+    table: Tuple[float, ...] = ()
 
 
 @dataclasses.dataclass
@@ -153,11 +169,22 @@ def parse_inputs_text(text: str) -> QMSInputs:
     trajs = []
     for axis in "XYZ":                                                        # F:134-151
         kind = _i(r.read(1, "trajectory type")[0], "trajectory type")
-        if kind != 1:
+        if kind == 1:
+            v0, a, n = r.read(3, "trajectory")
+            trajs.append(Trajectory(kind, _f(v0, "initial velocity"), _f(a, "acceleration"),
+                                    _i(n, "acceleration steps")))
+        elif kind == 2:
+            amp, f, ph = r.read(3, "harmonic trajectory")
+            trajs.append(Trajectory(kind, amp=_f(amp, "velocity amplitude"), freq=_f(f, "motion frequency"),
+                                    phase=_f(ph, "motion phase")))
+        elif kind == 3:
+            npts = _i(r.read(1, "velocity table length")[0], "velocity table length")
+            if npts < 1:
+                raise InputError(f"velocity table in {axis} direction needs at least one value")
+            table = tuple(_f(t, "velocity table") for t in r.read(npts, "velocity table"))
+            trajs.append(Trajectory(kind, table=table))
+        else:
             raise InputError(f"ERROR: TYPE OF TRAJECTORY IN {axis} DIRECTION IS NOT SUPPORTED")
-        v0, a, n = r.read(3, "trajectory")
-        trajs.append(Trajectory(kind, _f(v0, "initial velocity"), _f(a, "acceleration"),
-                                _i(n, "acceleration steps")))
     nmat = _i(r.read(1, "num_materials")[0], "num_materials")                 # F:153
     mats = []
     for _ in range(max(nmat, 0)):                                             # F:157-161

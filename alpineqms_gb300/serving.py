@@ -209,6 +209,48 @@ class QMSServer:
         return [self._results[k] for k in sorted(self._results)]
 
 
+def request_struct(i, geom, keep_slices: bool, precision: int):
+    """The qms_request of one solve (include/qms.h) and the arrays its pointers borrow: the
+    caller keeps the second value alive until the request is submitted (the server copies
+    them at submit)."""
+    from . import _lib as lib
+    r = lib.QmsRequest()
+    r.xs, r.ys, r.zs = i.xs, i.ys, i.zs
+    r.dx, r.dy, r.dz, r.dt = i.dx, i.dy, i.dz, i.dt
+    r.nt, r.tt = i.nt, i.tt
+    r.slice_axis = {"x": 0, "y": 1, "z": 2}[i.slice_axis]
+    r.slice_index = i.slice_index
+    r.keep = lib.QMS_KEEP_SLICES if keep_slices else lib.QMS_KEEP_NONE
+    r.precision = precision
+    for c in range(3):
+        r.B[c] = float(i.B[c])
+    for c, g in enumerate(np.asarray(i.G, dtype=np.float64).reshape(9)):
+        r.G[c] = float(g)
+    keep = []
+    for d, t in enumerate(i.traj):
+        r.traj_kind[d] = int(t.kind)
+        if t.kind == 2:
+            r.traj[d][0], r.traj[d][1], r.traj[d][2] = float(t.amp), float(t.freq), float(t.phase)
+        elif t.kind == 3:
+            tab = np.ascontiguousarray(t.table, dtype=np.float64)
+            keep.append(tab)
+            r.traj_table[d], r.traj_len[d] = tab.ctypes.data, tab.size
+        else:
+            r.traj[d][0], r.traj[d][1], r.traj[d][2] = float(t.v0), float(t.accel), float(t.n_accel)
+    if i.excitation is None:
+        r.exc_kind = lib.QMS_EXC_NONE
+    else:
+        kind, f, ph = i.excitation
+        r.exc_kind = lib.QMS_EXC_COS if kind == "cos" else lib.QMS_EXC_SIN
+        r.exc_f, r.exc_phase = float(f), float(ph)
+    if geom is not None:
+        g = np.ascontiguousarray(geom, dtype=np.float64)
+        table = np.ascontiguousarray(i.props_table(), dtype=np.float64)
+        keep += [g, table]
+        r.geom, r.table, r.nmat = g.ctypes.data, table.ctypes.data, table.shape[0]
+    return r, keep
+
+
 class NativeServer:
     """The serving object of libqms_gb300 (``qms_srv_*`` in include/qms.h): the same FIFO
     admission under an HBM budget and slot limit as QMSServer, with the admission and
@@ -233,30 +275,7 @@ class NativeServer:
 
     def submit(self, req: SolveRequest) -> int:
         ct, lib = self._ct, self._lib
-        i = req.inputs
-        r = lib.QmsRequest()
-        r.xs, r.ys, r.zs = i.xs, i.ys, i.zs
-        r.dx, r.dy, r.dz, r.dt = i.dx, i.dy, i.dz, i.dt
-        r.nt, r.tt = i.nt, i.tt
-        r.slice_axis = {"x": 0, "y": 1, "z": 2}[i.slice_axis]
-        r.slice_index = i.slice_index
-        r.keep = lib.QMS_KEEP_SLICES if req.keep_fields == "slice" else lib.QMS_KEEP_NONE
-        r.precision = self.precision
-        for c in range(3):
-            r.B[c] = float(i.B[c])
-        for c, g in enumerate(np.asarray(i.G, dtype=np.float64).reshape(9)):
-            r.G[c] = float(g)
-        for d, t in enumerate(i.traj):
-            r.traj[d][0], r.traj[d][1], r.traj[d][2] = float(t.v0), float(t.accel), float(t.n_accel)
-        if i.excitation is None:
-            r.exc_kind = lib.QMS_EXC_NONE
-        else:
-            kind, f, ph = i.excitation
-            r.exc_kind = lib.QMS_EXC_COS if kind == "cos" else lib.QMS_EXC_SIN
-            r.exc_f, r.exc_phase = float(f), float(ph)
-        geom = np.ascontiguousarray(req.geom, dtype=np.float64)
-        table = np.ascontiguousarray(i.props_table(), dtype=np.float64)
-        r.geom, r.table, r.nmat = geom.ctypes.data, table.ctypes.data, table.shape[0]
+        r, keep_alive = request_struct(req.inputs, req.geom, req.keep_fields == "slice", self.precision)
         rid = ct.c_longlong()
         rc = self.L.qms_srv_submit(self.h, ct.byref(r), ct.byref(rid))   # copies geom and table
         if rc:

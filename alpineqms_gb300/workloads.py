@@ -155,7 +155,13 @@ def inputs_text(inp: QMSInputs) -> str:
         L.append(r3(row))
     for t in inp.traj:
         L.append(str(t.kind))
-        L.append(f"{float(t.v0)!r},{float(t.accel)!r},{int(t.n_accel)}")
+        if t.kind == 2:
+            L.append(r3((t.amp, t.freq, t.phase)))
+        elif t.kind == 3:
+            L.append(str(len(t.table)))
+            L.append(",".join(repr(float(v)) for v in t.table))
+        else:
+            L.append(f"{float(t.v0)!r},{float(t.accel)!r},{int(t.n_accel)}")
     L.append(str(len(inp.materials)))
     for m in inp.materials:
         L.append(repr(float(m.mat_id)))

@@ -302,12 +302,21 @@ typedef struct {
     int precision;           /* QMS_PREC_* */
     double B[3];             /* background field (line 8) */
     double G[9];             /* its gradient, row-major (lines 9-11) */
-    double traj[3][3];       /* per axis: v0, acceleration, n_acc of trajectory type 1 (line 12) */
+    double traj[3][3];       /* per axis: v0, acceleration, n_acc of trajectory type 1 (line 12);
+                                amplitude, f, phase of type 2 */
     int exc_kind;            /* QMS_EXC_*: B and G scaled by cos/sin(2 pi f t + phase) */
     double exc_f, exc_phase;
     const double* geom;      /* xs*ys*zs float64 material IDs, Fortran order (copied at submit) */
     const double* table;     /* nmat x 7: ID, mu_r xyz, sigma xyz (copied at submit) */
     int nmat;
+    /* Trajectory type per axis: 0 or 1 = the reference's type 1 (F:136-150); 2 = harmonic,
+     * v(n) = amplitude sin(2 pi f n dt + phase); 3 = a velocity table of traj_len[d] values,
+     * v(n) = traj_table[d][min(n, len - 1)] (copied at submit).  Types 2 and 3 extend the
+     * reference, which stops on any type but 1 (F:135-151); the first-step pad applies to
+     * type-1 axes only. */
+    int traj_kind[3];
+    const double* traj_table[3];
+    int traj_len[3];
 } qms_request;
 
 enum { QMS_SRV_QUEUED = 0, QMS_SRV_RUNNING = 1, QMS_SRV_DONE = 2, QMS_SRV_FAILED = 3, QMS_SRV_REJECTED = 4 };
@@ -351,6 +360,9 @@ const char* qms_srv_error(qms_server* s, long long id);
 int qms_srv_stats_get(qms_server* s, qms_srv_stats* out);
 /* Waits for every queued and running request, then frees the server. */
 void qms_srv_destroy(qms_server* s);
+/* The frame velocities a request's solve uses (host only, no device work): out[0..2] for the
+ * steady state, out[3n..3n+2] for step n = 1..nsteps ((nsteps + 1) x 3 values). */
+int qms_srv_velocities(const qms_request* r, int nsteps, double* out);
 
 #ifdef __cplusplus
 }

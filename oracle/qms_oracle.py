@@ -270,7 +270,10 @@ def simulate(p, geom, steps=None, on_step=None, keep_states=False):
     """Run the reference algorithm on CPU with a direct solver.
 
     p: dict with xs, ys, zs, dx, dy, dz, dt, Nt, B (3), G (3x3), traj (3 x (v0, a, nacc)),
-       props (nmat, 7), optional excitation (kind, f, phase).
+       props (nmat, 7), optional excitation (kind, f, phase).  An optional ``velocities``
+       array ((steps + 1) x 3: the steady state's, then each step's) replaces the type-1
+       trajectory: the frame motions the reference stops on (F:135-151) enter its
+       assembly the same way, as one velocity per axis and step (F:431-433, F:1447-1449).
     Yields nothing; calls on_step(counter, x, H) for the steady state (counter 0)
     and each transient step.  Returns the list of (counter, x, H) if keep_states.
     """
@@ -291,7 +294,12 @@ def simulate(p, geom, steps=None, on_step=None, keep_states=False):
             return B0, G0
         return B0 * s, G0 * s
 
-    v = np.array([trajectory(traj[d][0], traj[d][1], int(traj[d][2]), 0, dt) for d in range(3)])
+    vel = p.get("velocities")
+    if vel is not None:
+        vel = np.asarray(vel, np.float64).reshape(-1, 3)
+        v = vel[0].copy()
+    else:
+        v = np.array([trajectory(traj[d][0], traj[d][1], int(traj[d][2]), 0, dt) for d in range(3)])
     Bs, Gs = scaled(0.0)
     ia, ja, a, b = assemble(xs, ys, zs, dx, dy, dz, coefs, False, dt, v, Bs, Gs)
     ds = DirectSolver()
@@ -308,7 +316,10 @@ def simulate(p, geom, steps=None, on_step=None, keep_states=False):
     for counter in range(1, nt + 1):
         nv = np.empty(3)
         for d in range(3):
-            nv[d], acc[d] = step_velocity(traj[d][0], traj[d][1], int(traj[d][2]), counter, dt, v[d], acc[d])
+            if vel is not None:
+                nv[d] = vel[counter, d]
+            else:
+                nv[d], acc[d] = step_velocity(traj[d][0], traj[d][1], int(traj[d][2]), counter, dt, v[d], acc[d])
         v = nv
         Bs, Gs = scaled(counter * dt)
         ia, ja, a, b = assemble(xs, ys, zs, dx, dy, dz, coefs, True, dt, v, Bs, Gs, x)

@@ -189,6 +189,44 @@ def _conductor_case(moving):
     return p, geom.flatten(order="F")
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_harmonic_and_tabulated_motion_vs_direct_oracle(precision):
+    """Trajectory types 2 (harmonic, along x) and 3 (a velocity table, along y), which the
+    reference stops on (F:135-151): the frame velocity changes every step, and every step's A,
+    H and sigma grad V must match the oracle's direct solve with the same velocities to 1e-8."""
+    from alpineqms_gb300.inputs import Trajectory
+    from alpineqms_gb300.trajectory import VelocitySchedule
+    p, geom = _conductor_case(True)
+    traj = [Trajectory(2, amp=10.0, freq=1e4, phase=0.5), Trajectory(3, table=(0.0, 3.0, -4.0, 5.0)),
+            Trajectory(1, 0.0, 0.0, 0)]
+    steps = 5
+    sched = VelocitySchedule(traj, p["dt"])
+    vel = np.array([sched.steady()] + [sched.step(n) for n in range(1, steps + 1)])
+    assert len({tuple(v) for v in vel[1:]}) == steps             # a new operator every step
+    ref = o.simulate(dict(p, velocities=vel), geom, steps=steps, keep_states=True)
+    s = solver_for(p["xs"], p["ys"], p["zs"], (p["dx"], p["dy"], p["dz"]), p["dt"], geom, p["props"],
+                   precision=precision)
+    B, G = np.asarray(p["B"], np.float64), np.asarray(p["G"], np.float64).ravel()
+    sched = VelocitySchedule(traj, p["dt"])
+    c = o.materials(p["xs"], p["ys"], p["zs"], geom, p["props"])
+    oV = o.block_offsets(p["xs"], p["ys"], p["zs"])[3]
+    for n, (counter, xr, Hr) in enumerate(ref):
+        v = sched.steady() if n == 0 else sched.step(n)
+        assert np.array_equal(v, vel[n])
+        st = s.steady(v, B, G) if n == 0 else s.step(v, B, G)
+        assert st["status"] == 0, (n, st)
+        x = s.get_state()
+        H = [h.ravel(order="F") for h in s.fields()]
+        assert rel_l2(x[:oV], xr[:oV]) <= 1e-8, (n, rel_l2(x[:oV], xr[:oV]))
+        for q in range(3):
+            assert rel_l2(H[q], Hr[q]) <= 1e-8, (n, q)
+        jv = o.edge_current_from_v(p["xs"], p["ys"], p["zs"], p["dx"], p["dy"], p["dz"], c, x)
+        jr = o.edge_current_from_v(p["xs"], p["ys"], p["zs"], p["dx"], p["dy"], p["dz"], c, xr)
+        if np.linalg.norm(jr) > 0:
+            assert rel_l2(jv, jr) <= 1e-8, (n, rel_l2(jv, jr))
+    s.close()
+
+
 @pytest.mark.parametrize("moving", [False, True])
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("precond", [1, 0], ids=["mg", "jacobi"])

@@ -64,7 +64,10 @@ def test_excitation_line():
 
 
 @pytest.mark.parametrize("old,new,msg", [
-    ("1\n0,-1e6,1\n", "2\n0,-1e6,1\n", "ERROR: TYPE OF TRAJECTORY IN X DIRECTION IS NOT SUPPORTED"),
+    ("1\n0,-1e6,1\n", "4\n0,-1e6,1\n", "ERROR: TYPE OF TRAJECTORY IN X DIRECTION IS NOT SUPPORTED"),
+    ("1\n0,0,0\n1\n0,0,0\n2\n", "1\n0,0,0\n0\n0,0,0\n2\n",
+     "ERROR: TYPE OF TRAJECTORY IN Z DIRECTION IS NOT SUPPORTED"),
+    ("1\n0,-1e6,1\n", "3\n0\n", "at least one value"),
     ("z,16", "w,16", "slice axis"),
     ("z,16", "z,25", "slice index"),
     ("\n2\nz,16", "\n0\nz,16", "tt"),
@@ -76,6 +79,21 @@ def test_rejected_inputs(old, new, msg):
     assert old in VALID
     with pytest.raises(InputError, match=msg):
         parse_inputs_text(VALID.replace(old, new, 1))
+
+
+def test_trajectory_types_beyond_one():
+    """Type 2 (harmonic: amplitude, f, phase) and type 3 (a velocity table: its length, then a
+    record of that many values over any number of lines) extend the reference's type 1."""
+    text = VALID.replace("1\n0,-1e6,1\n1\n0,0,0\n", "2\n0.5,2000,0.25\n3\n4\n0.0,1.0\n2.0, 3.0\n", 1)
+    inp = parse_inputs_text(text)
+    tx, ty, tz = inp.traj
+    assert (tx.kind, tx.amp, tx.freq, tx.phase) == (2, 0.5, 2000.0, 0.25)
+    assert (ty.kind, ty.table) == (3, (0.0, 1.0, 2.0, 3.0))
+    assert tz.kind == 1
+    assert inp.props_table().shape == (2, 7) and inp.geom_name == "geom.bin"
+    from alpineqms_gb300.workloads import inputs_text
+    back = parse_inputs_text(inputs_text(inp))               # the writer's grammar reads back
+    assert back.traj == inp.traj
 
 
 def test_truncated_file_and_terminator():

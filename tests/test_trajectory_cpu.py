@@ -46,3 +46,50 @@ def test_excitation():
     b1, g1 = scaled_field(B, G, ("cos", 1000.0, 0.0), 2.5e-4)
     s = excitation_scale(("cos", 1000.0, 0.0), 2.5e-4)
     assert np.array_equal(b1, np.asarray(B) * s) and np.array_equal(g1, G * s)
+
+
+MIXED = [Trajectory(2, amp=0.75, freq=2500.0, phase=0.3),      # harmonic
+         Trajectory(3, table=(0.0, 1.5, -2.0, 4.0)),             # a table, held after its end
+         Trajectory(1, 2.5, 0.0, 3)]                              # type 1 with the pad
+
+
+def test_schedule_types_two_and_three():
+    """Harmonic and tabulated axes follow their formulas; only the type-1 axis gets the
+    first-step pad, and it gets the same pad as in a pure type-1 schedule."""
+    import math
+    dt = 1e-5
+    sched = VelocitySchedule(MIXED, dt)
+    pure = VelocitySchedule([Trajectory(1, 2.5, 0.0, 3)] * 3, dt)
+    v = [sched.steady()] + [sched.step(n) for n in range(1, 9)]
+    w = [pure.steady()] + [pure.step(n) for n in range(1, 9)]
+    for n in range(9):
+        assert v[n][0] == 0.75 * math.sin(2.0 * math.pi * 2500.0 * (n * dt) + 0.3)
+        assert v[n][1] == (0.0, 1.5, -2.0, 4.0)[min(n, 3)]
+        assert v[n][2] == w[n][2]
+    assert v[1][2] != v[0][2]                                    # the pad moved the first step
+
+
+@pytest.mark.parametrize("traj", [MIXED, [Trajectory(1, *t) for t in TRAJS[2]]])
+def test_server_schedule_matches_python(traj):
+    """The native server's schedule (qms_srv_velocities, host only) equals the drop-in's."""
+    import ctypes
+    from alpineqms_gb300 import _lib, build as b
+    from alpineqms_gb300.inputs import parse_inputs_text
+    from alpineqms_gb300.serving import request_struct
+    from alpineqms_gb300.workloads import inputs_text, plain_block_32
+    b.build()
+    L = _lib.load()
+    inp, _ = plain_block_32(nt=12)
+    inp.traj = tuple(traj)
+    inp = parse_inputs_text(inputs_text(inp))                  # through the file grammar
+    r, keep = request_struct(inp, None, False, 0)
+    nsteps = 12
+    out = np.zeros((nsteps + 1, 3))
+    assert L.qms_srv_velocities(ctypes.byref(r), nsteps, out.ctypes.data) == 0
+    sched = VelocitySchedule(inp.traj, inp.dt)
+    want = np.array([sched.steady()] + [sched.step(n) for n in range(1, nsteps + 1)])
+    assert np.array_equal(out, want), np.abs(out - want).max()
+    bad, keep2 = request_struct(inp, None, False, 0)
+    bad.traj_kind[1] = 3
+    bad.traj_len[1] = 0
+    assert L.qms_srv_velocities(ctypes.byref(bad), nsteps, out.ctypes.data) == -1     # QMS_ERR_ARG
