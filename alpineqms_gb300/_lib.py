@@ -43,7 +43,7 @@ class QmsDesc(ctypes.Structure):
                 ("mg_coarse_sweeps", ctypes.c_int), ("mg_v_sweeps", ctypes.c_int),
                 ("mg_tail_points", ctypes.c_int), ("extrapolate", ctypes.c_int),
                 ("mg_v_coarse_cut", ctypes.c_double), ("gm_first_extend", ctypes.c_int),
-                ("tol_v", ctypes.c_double)]
+                ("tol_v", ctypes.c_double), ("start_ls", ctypes.c_int)]
 
 
 class QmsStats(ctypes.Structure):
@@ -51,7 +51,9 @@ class QmsStats(ctypes.Structure):
                 ("inner_iterations", ctypes.c_int),
                 ("initial_residual", ctypes.c_double),
                 ("final_residual", ctypes.c_double),
-                ("status", ctypes.c_uint), ("step_graph", ctypes.c_int)]
+                ("status", ctypes.c_uint), ("step_graph", ctypes.c_int),
+                ("start_ls", ctypes.c_int), ("start_coef", ctypes.c_double * 4),
+                ("start_base", ctypes.c_double), ("start_pred", ctypes.c_double)]
 
 
 class QmsProfile(ctypes.Structure):

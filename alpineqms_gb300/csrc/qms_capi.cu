@@ -54,6 +54,7 @@ void qms_default_desc(qms_desc* d, int xs, int ys, int zs, double dx, double dy,
     d->mg_coupling = 1;
     d->extrapolate = 3;
     d->gm_first_extend = 0;
+    d->start_ls = 4;
 }
 
 size_t qms_device_bytes(const qms_desc* d) { return d ? qms_device_bytes_impl(*d) : 0; }
@@ -73,6 +74,7 @@ int qms_create(const qms_desc* d, qms_handle** out) {
     if (dd.mg_coarse_sweeps < 0) dd.mg_coarse_sweeps = 0;
     if (dd.mg_v_sweeps < 0) dd.mg_v_sweeps = 0;
     dd.extrapolate = std::max(0, std::min(dd.extrapolate, 3));
+    dd.start_ls = std::max(0, std::min(dd.start_ls, 4));
     if (dd.max_inner <= 0 || dd.max_outer < 0 || !(dd.tol > 0) || !(dd.inner_rtol > 0) || dd.mg_sweeps < 1 ||
         !(dd.mg_omega > 0)) {
         std::lock_guard<std::mutex> lk(g_err_mu);

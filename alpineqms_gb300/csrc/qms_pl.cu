@@ -364,11 +364,23 @@ struct QStartRhs {
 // dp (optional): the pointers of the history buffers that rotate from step to step, read from
 // device memory instead of the arguments (a step captured in a CUDA graph replays with the
 // pointers of the step it runs)
+//
+// LS (the first pass of the least-squares start, qms_launch_step_start): r0 and w as above, x and
+// the residual left alone; instead each block sums, for the ls directions of the difference basis
+//   u1 = w,  u2 = w - w1,  u3 = w - 2 w1 + w2,  u4 = w - 3 w1 + 3 w2 - w3
+// (the residual images of d_n and of its backward differences: nearly independent, unlike the
+// w themselves), the Gram matrix u_i . u_j, the products u_i . r_b with the residual r_b of the
+// polynomial start of order min(ls, 3) (r_b = r0 - u1 - u2 - u3), and r_b . r_b, into lsp
+// (QMS_LS_SUMS x nb, quantity-major).  Products of the float high words, summed per thread in
+// float and across the block in double: the solve only needs the coefficients to a few digits,
+// because the apply pass forms the residual of the start it writes exactly (by linearity).
+template <bool LS>
 __global__ void __launch_bounds__(256) qk_step_start(
     QGrid g, qdf* __restrict__ rfin, const double* b_a, const double* bprev_a, const qdf* __restrict__ dinv,
     qdf* __restrict__ r0, double* __restrict__ x, const double* xo1_a, const double* xo2_a, const double* xo3_a,
     const int xo, qdf* wnew_a, const qdf* w1_a, const qdf* w2_a, float* __restrict__ rfloat,
-    double* __restrict__ partials, const QStartRhs R, const QStepPtrs* __restrict__ dp) {
+    double* __restrict__ partials, const QStartRhs R, const QStepPtrs* __restrict__ dp, const qdf* w3_a,
+    double* __restrict__ lsp) {
     __shared__ qdf prod[3][64];
     const QPL L = qms_pl(g);
     const int c = threadIdx.x >> 6, lane = threadIdx.x & 63;
@@ -383,7 +395,13 @@ __global__ void __launch_bounds__(256) qk_step_start(
     const qdf* __restrict__ w2 = dp ? dp->w2 : w2_a;
     const double* __restrict__ hx = dp ? dp->hx : R.hx;
     const double* __restrict__ sg = R.sg;
+    const qdf* __restrict__ w3 = dp ? dp->w3 : w3_a;
     float racc = 0.f, xacc = 0.f;
+    float ls_acc[QMS_LS_SUMS];
+    if constexpr (LS) {
+#pragma unroll
+        for (int q = 0; q < QMS_LS_SUMS; q++) ls_acc[q] = 0.f;
+    }
     for (unsigned base = blockIdx.x * 64u; base < Nn; base += gridDim.x * 64u) {
         const unsigned t = base + lane;
         const bool valid = t < Nn;
@@ -440,6 +458,26 @@ __global__ void __launch_bounds__(256) qk_step_start(
         }
         r0[pl] = a;
         if (R.x0) R.x0[ref] = xs;
+        if constexpr (LS) {
+            // xo = ls >= 1 directions; wnew is formed (w)
+            const qdf v1 = xo >= 2 ? w1[pl] : qdf(), v2 = xo >= 3 ? w2[pl] : qdf(), v3 = xo >= 4 ? w3[pl] : qdf();
+            const qdf e1 = v1 - v2, e2 = e1 - (v2 - v3);          // w1 - w2, w1 - 2 w2 + w3
+            const qdf u2 = w - v1, u3 = u2 - e1, u4 = u3 - e2;
+            qdf base_r = a - w;
+            if (xo >= 2) base_r = base_r - u2;
+            if (xo >= 3) base_r = base_r - u3;
+            const float u[4] = {w.h, xo >= 2 ? u2.h : 0.f, xo >= 3 ? u3.h : 0.f, xo >= 4 ? u4.h : 0.f};
+            const float rb = base_r.h;
+            int q = 0;
+#pragma unroll
+            for (int i0 = 0; i0 < 4; i0++)
+#pragma unroll
+                for (int j0 = i0; j0 < 4; j0++) ls_acc[q++] += u[i0] * u[j0];
+#pragma unroll
+            for (int i0 = 0; i0 < 4; i0++) ls_acc[10 + i0] += u[i0] * rb;
+            ls_acc[14] += rb * rb;
+            continue;
+        }
         if (ex) {
             xs = qms_extrap(xo, xs, x1, xo >= 2 ? xo2[ref] : 0.0, xo >= 3 ? xo3[ref] : 0.0);
             x[ref] = xs;
@@ -456,7 +494,179 @@ __global__ void __launch_bounds__(256) qk_step_start(
             xacc += f * f;
         }
     }
+    __shared__ double sh[32];
+    const long long nb = gridDim.x;
+    if constexpr (LS) {
+#pragma unroll
+        for (int q = 0; q < QMS_LS_SUMS; q++) {
+            const double t = qBlockSum(ls_acc[q], sh);
+            if (threadIdx.x == 0) lsp[q * nb + blockIdx.x] = t;
+        }
+        return;
+    }
     if (!rfloat) return;
+    double s = qBlockSum(c < 3 ? racc : 0.f, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+    s = qBlockSum(c < 3 ? 0.f : racc, sh);
+    if (threadIdx.x == 0) partials[nb + blockIdx.x] = s;
+    s = qBlockSum(c < 3 ? xacc : 0.f, sh);
+    if (threadIdx.x == 0) partials[2 * nb + blockIdx.x] = s;
+    s = qBlockSum(c < 3 ? 0.f : xacc, sh);
+    if (threadIdx.x == 0) partials[3 * nb + blockIdx.x] = s;
+}
+
+// The coefficients of the least-squares start from the partial sums of its first pass (one
+// block): the sums over the blocks in a fixed order, then the normal equations G c = h of the
+// ls directions of the difference basis, scaled to a unit diagonal and solved by Cholesky; a
+// direction whose pivot falls below 1e-5 (numerically dependent at the float accuracy of the
+// sums) gets no coefficient.  The start is the polynomial one (base coefficients 1 on
+// u1..u_min(ls,3)) plus c; out[0..3] = its coefficients g_j on d_1..d_4 (g = T^T (base + c) for the
+// map u = T w), out[4] = |r_b|^2, out[5] = the predicted |r|^2 of the start, out[6] = the
+// directions used.  Non-finite sums leave the polynomial start.
+__global__ void __launch_bounds__(256) qk_ls_solve(const double* __restrict__ lsp, long long nb, int ls,
+                                                  double* __restrict__ out) {
+    __shared__ double sh[32];
+    __shared__ double tot[QMS_LS_SUMS];
+    for (int q = 0; q < QMS_LS_SUMS; q++) {
+        double t = 0.0;
+        for (long long b = threadIdx.x; b < nb; b += blockDim.x) t += lsp[q * nb + b];
+        t = qBlockSum(t, sh);
+        if (threadIdx.x == 0) tot[q] = t;
+    }
+    if (threadIdx.x != 0) return;
+    double G[4][4], h[4], sc[4], A[4][4], L[4][4], z[4], c[4];
+    int q = 0;
+    for (int i = 0; i < 4; i++)
+        for (int j = i; j < 4; j++) { G[i][j] = tot[q]; G[j][i] = tot[q]; q++; }
+    for (int i = 0; i < 4; i++) h[i] = tot[10 + i];
+    const double rb2 = tot[14];
+    bool on[4];
+    for (int i = 0; i < 4; i++) {
+        on[i] = i < ls && G[i][i] > 0.0 && isfinite(G[i][i]) && isfinite(h[i]);
+        sc[i] = on[i] ? sqrt(G[i][i]) : 1.0;
+    }
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) A[i][j] = on[i] && on[j] ? G[i][j] / (sc[i] * sc[j]) : (i == j ? 1.0 : 0.0);
+    int used = 0;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) L[i][j] = 0.0;
+    for (int k = 0; k < 4; k++) {
+        if (!on[k]) { L[k][k] = 1.0; z[k] = 0.0; continue; }
+        double d = A[k][k];
+        for (int m = 0; m < k; m++) d -= L[k][m] * L[k][m];
+        if (!(d > 1e-5)) {                       // dependent on the directions before it
+            on[k] = false;
+            L[k][k] = 1.0;
+            z[k] = 0.0;
+            continue;
+        }
+        L[k][k] = sqrt(d);
+        for (int i = k + 1; i < 4; i++) {
+            if (!on[i]) continue;
+            double t = A[i][k];
+            for (int m = 0; m < k; m++) t -= L[i][m] * L[k][m];
+            L[i][k] = t / L[k][k];
+        }
+        double t = h[k] / sc[k];
+        for (int m = 0; m < k; m++) t -= L[k][m] * z[m];
+        z[k] = t / L[k][k];
+        used++;
+    }
+    for (int k = 3; k >= 0; k--) {
+        double t = z[k];
+        for (int m = k + 1; m < 4; m++) t -= L[m][k] * c[m];
+        c[k] = on[k] ? t / L[k][k] : 0.0;
+    }
+    bool ok = true;
+    for (int k = 0; k < 4; k++) { c[k] = on[k] ? c[k] / sc[k] : 0.0; ok = ok && isfinite(c[k]); }
+    double pred = rb2;
+    if (ok) {
+        for (int i = 0; i < 4; i++) {
+            pred -= 2.0 * c[i] * h[i];
+            for (int j = 0; j < 4; j++) pred += c[i] * G[i][j] * c[j];
+        }
+    }
+    if (!ok) {
+        for (int k = 0; k < 4; k++) c[k] = 0.0;
+        pred = rb2;
+        used = 0;
+    }
+    const int p = ls < 3 ? ls : 3;              // the polynomial base
+    double u[4];
+    for (int k = 0; k < 4; k++) u[k] = (k < p ? 1.0 : 0.0) + c[k];
+    out[0] = u[0] + u[1] + u[2] + u[3];
+    out[1] = -u[1] - 2.0 * u[2] - 3.0 * u[3];
+    out[2] = u[2] + 3.0 * u[3];
+    out[3] = -u[3];
+    out[4] = rb2;
+    out[5] = pred;
+    out[6] = (double)used;
+}
+
+// The second pass of the least-squares start: with the coefficients g (qk_ls_solve)
+//   x = x_n + sum_j g_j d_j   (the rows that are not Dirichlet rows)
+//   r = r0 - sum_j g_j w_j    (w_1 = w, the one this step formed; in double-float)
+// into x, rfin, rfloat (FP32) and the partials |r_A|^2, |r_V|^2, |x_A|^2, |x_V|^2 of the launch's
+// blocks, the layout and block shape of qk_step_start.
+__global__ void __launch_bounds__(256) qk_start_apply(
+    QGrid g, double* __restrict__ x, const double* xo1_a, const double* xo2_a, const double* xo3_a,
+    const double* xo4_a, const int ls, const qdf* __restrict__ r0, const qdf* wnew_a, const qdf* w1_a,
+    const qdf* w2_a, const qdf* w3_a, const double* __restrict__ coef, qdf* __restrict__ rfin,
+    float* __restrict__ rfloat, double* __restrict__ partials, const QStepPtrs* __restrict__ dp) {
+    const QPL L = qms_pl(g);
+    const int c = threadIdx.x >> 6, lane = threadIdx.x & 63;
+    const unsigned Nx = (unsigned)g.Nx, Nxy = (unsigned)g.Nx * (unsigned)g.Ny, Nn = (unsigned)g.Nn;
+    const double* __restrict__ xo1 = dp ? dp->xo1 : xo1_a;
+    const double* __restrict__ xo2 = dp ? dp->xo2 : xo2_a;
+    const double* __restrict__ xo3 = dp ? dp->xo3 : xo3_a;
+    const double* __restrict__ xo4 = dp ? dp->xo4 : xo4_a;
+    const qdf* __restrict__ w0 = dp ? dp->wnew : wnew_a;
+    const qdf* __restrict__ w1 = dp ? dp->w1 : w1_a;
+    const qdf* __restrict__ w2 = dp ? dp->w2 : w2_a;
+    const qdf* __restrict__ w3 = dp ? dp->w3 : w3_a;
+    const double g1 = coef[0], g2 = coef[1], g3 = coef[2], g4 = coef[3];
+    const qdf q1 = qdf_split(g1), q2 = qdf_split(g2), q3 = qdf_split(g3), q4 = qdf_split(g4);
+    float racc = 0.f, xacc = 0.f;
+    for (unsigned base = blockIdx.x * 64u; base < Nn; base += gridDim.x * 64u) {
+        const unsigned t = base + lane;
+        if (t >= Nn) continue;
+        const unsigned kk = t / Nxy, rem = t - kk * Nxy, jj = rem / Nx;
+        const int i = (int)(rem - jj * Nx) + 1, j = (int)jj + 1, k = (int)kk + 1;
+        bool has, fix;
+        long long ref;
+        if (c == 0) { has = i <= g.xs; ref = has ? qAX(g, i, j, k) : 0; fix = qFixX(g, i, j, k); }
+        else if (c == 1) { has = j <= g.ys; ref = has ? qAY(g, i, j, k) : 0; fix = qFixY(g, i, j, k); }
+        else if (c == 2) { has = k <= g.zs; ref = has ? qAZ(g, i, j, k) : 0; fix = qFixZ(g, i, j, k); }
+        else { has = true; ref = qV(g, i, j, k); fix = qFixV(g, i, j, k); }
+        if (!has) continue;
+        const long long pl = c * L.comp + qms_pl_node(g, L, i, j, k);
+        qdf s = q1 * w0[pl];
+        if (ls >= 2) s = s + q2 * w1[pl];
+        if (ls >= 3) s = s + q3 * w2[pl];
+        if (ls >= 4) s = s + q4 * w3[pl];
+        const qdf r = r0[pl] - s;
+        double xs = x[ref];
+        if (!fix) {
+            const double x1 = xo1[ref];
+            double dx = g1 * (xs - x1);
+            if (ls >= 2) {
+                const double x2 = xo2[ref];
+                dx = fma(g2, x1 - x2, dx);
+                if (ls >= 3) {
+                    const double x3 = xo3[ref];
+                    dx = fma(g3, x2 - x3, dx);
+                    if (ls >= 4) dx = fma(g4, x3 - xo4[ref], dx);
+                }
+            }
+            xs += dx;
+            x[ref] = xs;
+        }
+        rfloat[pl] = r.h;
+        rfin[pl] = r;
+        racc += r.h * r.h;
+        const float f = qdf_split(xs).h;
+        xacc += f * f;
+    }
     __shared__ double sh[32];
     const long long nb = gridDim.x;
     double s = qBlockSum(c < 3 ? racc : 0.f, sh);
@@ -751,8 +961,17 @@ void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const dou
         R.idt[2] = qdf(1.0 / (h.dt * g.dz));
         R.x0 = h.x0;
     }
-    qk_step_start<<<(unsigned)nb, 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3, h.xo, h.wnew,
-                                                 h.w1, h.w2, rfloat, partials, R, dptrs);
+    if (h.ls > 0) {
+        qk_step_start<true><<<(unsigned)nb, 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3, h.ls,
+                                                           h.wnew, h.w1, h.w2, nullptr, partials, R, dptrs, h.w3, h.lsp);
+        qk_ls_solve<<<1, 256, 0, st>>>(h.lsp, nb, h.ls, h.lsg);
+        qk_start_apply<<<(unsigned)nb, 256, 0, st>>>(g, h.x, h.xo1, h.xo2, h.xo3, h.xo4, h.ls, r0, h.wnew, h.w1, h.w2,
+                                                     h.w3, h.lsg, rfin, rfloat, partials, dptrs);
+        return;
+    }
+    qk_step_start<false><<<(unsigned)nb, 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3, h.xo,
+                                                        h.wnew, h.w1, h.w2, rfloat, partials, R, dptrs, nullptr,
+                                                        nullptr);
 }
 
 void qms_launch_dinv_df(const QGrid& g, const QCoef<double>& c, const QStepPar<double>& P, qdf* out, cudaStream_t st) {

@@ -52,6 +52,15 @@ struct QStepStart {
     const double* sdt;
     double dt;
     double* x0;
+    // Least-squares start (ls > 0 directions, at most 4; xo = ls): x = x_n + sum_j g_j d_j with
+    // the coefficients g that minimise the scaled residual over the span of the last ls state
+    // differences d_j = x_{n-j+1} - x_{n-j}, whose residual images are w, w1, w2, w3; x_{n-4} in
+    // xo4.  lsp: 15 x nb partial sums, lsg: 8 doubles (the coefficients, then diagnostics).
+    const double* xo4;
+    const qdf* w3;
+    int ls;
+    double* lsp;
+    double* lsg;
 };
 // the history pointers that rotate from step to step, for a step start that reads them from
 // device memory (dptrs) instead of its arguments (with hx: the pointers are those of h)
@@ -65,7 +74,12 @@ struct QStepPtrs {
     const double* hx;
     const double* b;
     const double* bprev;
+    const double* xo4;
+    const qdf* w3;
 };
+// partial sums per block of the least-squares start (Gram matrix of 4 directions, their products
+// with the base residual, and the base residual's square)
+#define QMS_LS_SUMS 15
 // nb: the blocks of the launch and the partials per quantity
 void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
                            const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st,

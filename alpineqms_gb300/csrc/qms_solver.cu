@@ -574,7 +574,8 @@ void QmsSolver::release() {
     nc16 = nullptr;
     void* ptrs[] = {ids,   dtab64, dtab32,    x,     b,      r64,    xbest, H,   slicebuf, part,   S,
                     status, dg_steady, dg_tr, mgtmp, mgtmp2, nc32,  nc64,  xdf, r0df,     ncdf, rpl, x0,
-                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2, hist_x, xold3, wh[0], wh[1], wh[2]};
+                    rsg,   rsdt,   bprev,     rfin,  dinvdf, xold, xold2, hist_x, xold3, wh[0], wh[1], wh[2],
+                    wh[3], xold4, lsp, lsg};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (hS) cudaFreeHost(hS);
     if (hptrs) cudaFreeHost(hptrs);
@@ -602,7 +603,8 @@ void QmsSolver::release() {
     xdf = r0df = ncdf = nullptr; rpl = nullptr; x0 = nullptr; df_resid = false; anchor_ready = false;
     rsg = rsdt = nullptr;
     bprev = nullptr; rfin = dinvdf = nullptr; rfin_ok = false; chain_len = 0; xold = xold2 = nullptr;
-    hist_x = nullptr; hist_len = 0; xold3 = nullptr; wh[0] = wh[1] = wh[2] = nullptr; w_len = 0; last_chained = false;
+    hist_x = nullptr; hist_len = 0; xold3 = xold4 = nullptr; wh[0] = wh[1] = wh[2] = wh[3] = nullptr; w_len = 0;
+    nwh = 0; lsp = lsg = nullptr; last_chained = false;
     field_run = 0; start_resid_ready = false;
     nc32 = nullptr; nc64 = nullptr;
     for (auto& p : vec) p = nullptr;
@@ -691,9 +693,16 @@ int QmsSolver::init(const qms_desc& d) {
         CK(cudaMalloc(&bprev, n * 8));
         CK(cudaMalloc(&xold, n * 8));
         CK(cudaMalloc(&hist_x, n * 8));
-        if (d.extrapolate >= 2) CK(cudaMalloc(&xold2, n * 8));
-        if (d.extrapolate >= 3) CK(cudaMalloc(&xold3, n * 8));
-        for (int q = 0; q < std::min(d.extrapolate, 3); q++) CK(pl_alloc((void**)&wh[q], 8));
+        const int hx_need = std::max(std::min(d.extrapolate, 3), d.start_ls);   // history beyond x_n, x_(n-1)
+        if (hx_need >= 2) CK(cudaMalloc(&xold2, n * 8));
+        if (hx_need >= 3) CK(cudaMalloc(&xold3, n * 8));
+        if (hx_need >= 4) CK(cudaMalloc(&xold4, n * 8));
+        nwh = hx_need;
+        for (int q = 0; q < nwh; q++) CK(pl_alloc((void**)&wh[q], 8));
+        if (d.start_ls > 0) {
+            CK(cudaMalloc(&lsp, (size_t)QMS_LS_SUMS * nbop * 8));
+            CK(cudaMalloc(&lsg, 8 * 8));
+        }
         CK(pl_alloc((void**)&rfin, 8));
         CK(pl_alloc((void**)&dinvdf, 8));
         CK(cudaMalloc(&x0, n * 8));
@@ -743,9 +752,13 @@ size_t qms_device_bytes_impl(const qms_desc& d) {
     // the block-triangular preconditioner's V right-hand side; the double-float residual's x, b,
     // coefficients and FP32 result (mixed precision)
     size_t tri = d.precond == QMS_PRECOND_MG ? qms_pl(g).n * ts : 0;
+    // history of the extrapolated and least-squares starts: x_(n-2).. and the residual images
+    const int lsn = std::max(0, std::min(d.start_ls, 4));
+    const size_t hxn = (size_t)std::max(std::max(0, std::min(d.extrapolate, 3)), lsn);
     if (ts == 4) tri += (size_t)6 * qms_pl16_pitch(g) * g.Ny * g.Nz * 2;       // bf16 node coefficients
     if (ts == 4) tri += qms_pl(g).n * (8 + 8 + 4 + 8 + 8) + 6 * qms_pl(g).comp * 8 + 5 * g.n * 8 + 2 * g.oV * 8 +
-                        (d.extrapolate >= 3 ? g.n * 8 : 0) + std::max(0, std::min(d.extrapolate, 3)) * qms_pl(g).n * 8;
+                        (hxn > 2 ? hxn - 2 : 0) * g.n * 8 + hxn * qms_pl(g).n * 8 +
+                        (lsn > 0 ? (QMS_LS_SUMS * (size_t)qms_op_num_blocks(g) + 8) * 8 : 0);
     size_t ncell = (size_t)g.xs * g.ys * g.zs;
     size_t smax = std::max({(size_t)g.ys * g.zs, (size_t)g.xs * g.zs, (size_t)g.xs * g.ys});
     size_t nb = (size_t)qms_op_num_blocks(g);
@@ -767,6 +780,8 @@ int QmsSolver::set_materials(const uint8_t* host_slots, const double* rows6, int
     gm_k_fine = false;
     gm_k_floor = 0;
     gm_k_floor_age = 0;
+    gm_ls_floor = 0;
+    gm_ls_floor_age = 0;
     if (nmat < 0 || nmat > QMS_MAX_SLOTS - 1) { err = "nmat must be in 0..255"; return QMS_ERR_ARG; }
     const long long ncell = (long long)g.xs * g.ys * g.zs;
     if (host_slots) {
@@ -1215,7 +1230,7 @@ int QmsSolver::step_graph(bool adv, const double v[3], const QStepStart& hs, boo
     const bool dbx = hs.hx != nullptr;
     StepGraph* G = nullptr;
     for (StepGraph& e : sgraphs)
-        if (e.k == k && e.xo == hs.xo && e.wcalc == wcalc && e.dbx == dbx && e.v[0] == v[0] && e.v[1] == v[1] &&
+        if (e.k == k && e.xo == hs.xo && e.ls == hs.ls && e.wcalc == wcalc && e.dbx == dbx && e.v[0] == v[0] && e.v[1] == v[1] &&
             e.v[2] == v[2]) { G = &e; break; }
     if (!G) {
         constexpr size_t kMax = 4;
@@ -1289,13 +1304,13 @@ int QmsSolver::step_graph(bool adv, const double v[3], const QStepStart& hs, boo
             err = std::string("step graph: ") + cudaGetErrorString(e);
             return QMS_ERR_CUDA;
         }
-        ng.k = k; ng.xo = hs.xo; ng.wcalc = wcalc; ng.dbx = dbx;
+        ng.k = k; ng.xo = hs.xo; ng.ls = hs.ls; ng.wcalc = wcalc; ng.dbx = dbx;
         ng.v[0] = v[0]; ng.v[1] = v[1]; ng.v[2] = v[2];
         sgraphs.push_back(ng);
         G = &sgraphs.back();
     }
     // the rotating pointers of this step, read by the graph's copy node at launch
-    *hptrs = QStepPtrs{hs.xo1, hs.xo2, hs.xo3, hs.wnew, hs.w1, hs.w2, hs.hx, b, bprev};
+    *hptrs = QStepPtrs{hs.xo1, hs.xo2, hs.xo3, hs.wnew, hs.w1, hs.w2, hs.hx, b, bprev, hs.xo4, hs.w3};
     G->used = ++graph_clock;
     CK(cudaGraphLaunch(G->exec, st));
     int rc = read_scalars();                    // synchronises the stream
@@ -1392,7 +1407,7 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     const bool same_op = transient && chain_v[0] == v[0] && chain_v[1] == v[1] && chain_v[2] == v[2];
     if (!same_op) hist_len = 0;
     // order of the extrapolation: the known solutions (hist_len, x_n included) less one
-    const int xo = !same_op || !xold ? 0 : std::max(0, std::min(std::min(desc.extrapolate, 3), hist_len - 1));
+    int xo = !same_op || !xold ? 0 : std::max(0, std::min(std::min(desc.extrapolate, 3), hist_len - 1));
     bool same_field = true;
     for (int q = 0; q < 3; q++) same_field = same_field && chain_B[q] == B[q];
     for (int q = 0; q < 9; q++) same_field = same_field && chain_G[q] == G[q];
@@ -1401,6 +1416,13 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // residual of the extrapolated start then follows from the w of the last xo steps when the
     // Dirichlet values did not change over them
     const bool wcalc = chain && last_chained && wh[0];
+    // the least-squares start over ls of the last state differences: the known solutions less
+    // one, the stored residual images of the differences before d_n plus the one formed now,
+    // and the solves with the same Dirichlet values all bound it
+    int ls = 0;
+    if (wcalc && same_op && xold && desc.start_ls > 0)
+        ls = std::max(0, std::min(std::min(desc.start_ls, hist_len - 1), std::min(w_len + 1, field_run - 2)));
+    if (ls > 0) xo = ls;
     const bool start_fused = wcalc && xo > 0 && w_len >= xo - 1 && field_run >= xo + 2;
     // with the field unchanged and x_(n-1) known, the anchor takes b - b_prev from x_n - x_(n-1)
     // (the step start, in double-float) and this solve forms no FP64 right-hand side
@@ -1434,14 +1456,16 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     if (chain) {                   // ... unless it follows from the previous one
         // the anchor, w_n and the extrapolated start in one pass; the residual of that start too
         // when start_fused (otherwise the double-float residual from the anchor follows)
-        const int nw = std::min(desc.extrapolate, 3);          // w buffers: w_(n-1), w_(n-2), the new one
-        QStepStart hs{x,       xold, xold2, xold3, xo, wcalc ? wh[nw - 1] : nullptr, wh[0], wh[1],
-                      db_from_x ? hist_x : nullptr, rsg, rsdt, desc.dt, db_from_x ? x0 : nullptr};
+        const int nw = nwh;                                     // w buffers: w_(n-1), w_(n-2), ..., the new one
+        QStepStart hs{x,    xold, xold2, xold3, xo, wcalc ? wh[nw - 1] : nullptr, wh[0], wh[1],
+                      db_from_x ? hist_x : nullptr, rsg, rsdt, desc.dt, db_from_x ? x0 : nullptr,
+                      xold4, wh[2], ls, lsp, lsg};
         if (use_step_graph) {
             sg_hs = hs;                  // launched inside the step's graph below
             sg_wcalc = wcalc;
         } else {
-            OpEv* ev = start_fused ? prof_begin(3, (double)g.n * (8 * 11 + 8 * 2 * xo + 4)) : nullptr;
+            OpEv* ev = start_fused ? prof_begin(3, (double)g.n * (ls > 0 ? 8 * 11 + 8 * (ls - 1) + 8 * (2 * ls + 5) + 4
+                                                                         : 8 * 11 + 8 * 2 * xo + 4)) : nullptr;
             qms_launch_step_start(g, rfin, b, bprev, dinvdf, r0df, hs, start_fused ? rpl : nullptr, part, nbop, st);
             nlaunch++;
             prof_end(ev);
@@ -1618,13 +1642,14 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // history of converged transient solutions for the extrapolated start (x itself is the newest;
     // xold and xold2 the two before, rotated by pointer: only the extrapolation reads them)
     if (transient && rel <= desc.tol && xold) {
-        double* freed = xold3 ? xold3 : xold2 ? xold2 : xold;
+        double* freed = xold4 ? xold4 : xold3 ? xold3 : xold2 ? xold2 : xold;
+        if (xold4) xold4 = xold3;
         if (xold3) xold3 = xold2;
         if (xold2) xold2 = xold;
         xold = hist_x;
         hist_x = freed;
         CK(cudaMemcpyAsync(hist_x, x, g.n * 8, cudaMemcpyDeviceToDevice, st));
-        hist_len = std::min(hist_len + 1, xold3 ? 4 : xold2 ? 3 : 2);
+        hist_len = std::min(hist_len + 1, xold4 ? 5 : xold3 ? 4 : xold2 ? 3 : 2);
     } else {
         hist_len = 0;
         last_chained = false;
@@ -1652,7 +1677,31 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // One-replay solves probe down to 5 steps; a probe below 6 that needed a second replay goes
     // back to 6, which then holds for 32 solves.  (Letting any count step back up after a
     // second replay raised it instead: one slow step pinned it at 7-8 for 32 solves.)
-    if (graph_cycles > 0 && rel <= desc.tol) {
+    // After a least-squares start the start residual is within a few times the tolerance and
+    // falls from step to step, so the count follows the measured rate: a one-replay solve that
+    // ended below tol / 10 takes the count that this solve's reduction per FGMRES step says
+    // reaches tol / 10 from its start (at least one less); a solve that needed a second replay
+    // goes up by one (two after a third), and when its start had every direction it holds there
+    // for 4 solves (the first steps of a run know fewer directions and start worse: floors from
+    // them kept the count high well after).  Floors set by solves without this start do not apply.
+    if (graph_cycles > 0 && rel <= desc.tol && ls > 0) {
+        if (gm_ls_floor > 0 && ++gm_ls_floor_age > 4) { gm_ls_floor = 0; gm_ls_floor_age = 0; }
+        if (graph_cycles >= 2) {
+            gm_k_est = std::min(gm_m, gm_k_est + (graph_cycles >= 3 ? 2 : 1));
+            if (ls >= desc.start_ls) {
+                gm_ls_floor = gm_k_est;
+                gm_ls_floor_age = 0;
+            }
+        } else if (rel < desc.tol / 10.0) {
+            const double r0 = stats.initial_residual;
+            int need = 1;
+            if (r0 > desc.tol / 10.0 && rel > 0.0 && r0 > rel) {
+                const double rate = std::log(r0 / rel) / std::max(1, gm_k_est);
+                need = (int)std::ceil(std::log(r0 / (desc.tol / 10.0)) / rate);
+            }
+            gm_k_est = std::max(std::max(1, gm_ls_floor), std::min(gm_k_est - 1, need));
+        }
+    } else if (graph_cycles > 0 && rel <= desc.tol) {
         if (gm_k_floor > 0 && ++gm_k_floor_age >= 32) { gm_k_floor--; gm_k_floor_age = 0; }
         if (graph_cycles >= 3) {
             gm_k_floor = gm_k_est + 1;
@@ -1673,8 +1722,16 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
         }
     }
     unsigned stt = 0;
+    double lsv[8] = {};
     CK(cudaMemcpyAsync(&stt, status, 4, cudaMemcpyDeviceToHost, st));
+    if (ls > 0) CK(cudaMemcpyAsync(lsv, lsg, sizeof(lsv), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (ls > 0) {
+        stats.start_ls = ls;
+        for (int q = 0; q < 4; q++) stats.start_coef[q] = lsv[q];
+        stats.start_base = lsv[4];
+        stats.start_pred = lsv[5];
+    }
     stats.status |= stt & ~(unsigned)QMS_ST_BREAKDOWN;
     stats.outer_iterations = outer;
     stats.final_residual = rel;

@@ -80,12 +80,16 @@ struct QmsSolver {
     double* xold = nullptr;     // the one before it
     double* xold2 = nullptr;    // ... and the one before that (quadratic extrapolation)
     double* xold3 = nullptr;    // ... and the one before that (cubic)
-    int hist_len = 0;           // consecutive converged transient solves with the same operator (<= 4)
+    double* xold4 = nullptr;    // ... and the one before that (least-squares start over 4 differences)
+    int hist_len = 0;           // consecutive converged transient solves with the same operator (<= 5)
     // Residual of the extrapolated start by linearity (qk_step_start): w_n = D^-1 M (x_n - x_{n-1})
     // is the difference of a chained solve's anchor and final residual; wh[0] holds the last
-    // step's, wh[1] the one before (cubic), w_len of them valid; one more buffer takes the next
-    qdf* wh[3] = {nullptr, nullptr, nullptr};
+    // step's, wh[1] the one before (cubic), ..., w_len of them valid; one more buffer takes the next
+    qdf* wh[4] = {nullptr, nullptr, nullptr, nullptr};
     int w_len = 0;
+    int nwh = 0;                // w buffers allocated
+    double* lsp = nullptr;      // least-squares start: QMS_LS_SUMS x nbop partial sums
+    double* lsg = nullptr;      // ... and its coefficients and diagnostics (8 doubles)
     bool last_chained = false;  // the last solve's anchor state was the solution before it
     int field_run = 0;          // consecutive solves (this one included) with the same B, G
     bool start_resid_ready = false;   // the step start formed the first residual
@@ -208,7 +212,7 @@ struct QmsSolver {
     static constexpr int kStepGraphCycles = 3;
     struct StepGraph {
         cudaGraphExec_t exec = nullptr;
-        int k = 0, xo = 0;
+        int k = 0, xo = 0, ls = 0;
         bool wcalc = false, dbx = false;
         double v[3] = {0, 0, 0};
         long long pro = 0, body = 0;     // kernel launches of the prologue and of one cycle
@@ -223,6 +227,8 @@ struct QmsSolver {
     bool graph_resid_ready = false;
     int gm_k_est = 0;           // FGMRES iterations replayed per refinement iteration (0: not yet known)
     int gm_k_seen = 0;          // largest count seen while running with host checks
+    int gm_ls_floor = 0;        // lowest count for solves after a least-squares start, and its age
+    int gm_ls_floor_age = 0;
     bool gm_k_fine = false;     // gm_k_est has overshot downwards once: tune it in single steps
     int gm_k_floor = 0;         // smallest count not yet known to need a third replay
     int gm_k_floor_age = 0;     // solves since gm_k_floor was set or lowered

@@ -83,7 +83,8 @@ class QMSSolver:
         s = QmsStats()
         check(self.L.qms_get_stats(self.h, ctypes.byref(s)), self.h, "qms_get_stats")
         return dict(outer=s.outer_iterations, inner=s.inner_iterations, r0=s.initial_residual,
-                    r=s.final_residual, status=s.status, step_graph=s.step_graph)
+                    r=s.final_residual, status=s.status, step_graph=s.step_graph, start_ls=s.start_ls,
+                    start_coef=list(s.start_coef), start_base=s.start_base, start_pred=s.start_pred)
 
     def fields(self):
         """(Hx, Hy, Hz) cubes, each (xs, ys, zs) Fortran-ordered views."""

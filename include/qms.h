@@ -126,6 +126,11 @@ typedef struct {
                                 moving plate it kept longer single cycles, 30.6 vs 28.0 ms per step) */
     double tol_v;            /* > 0: a solve also stops only when ||r_V|| <= tol_v * ||x_V|| (the potential block's
                                 scaled residual against its own size); 0 = off (the default) */
+    int start_ls;            /* chained transient steps (mixed precision): the start is x_n plus the combination
+                                of the last start_ls (<= 4) state differences that minimises the
+                                scaled residual (found on the device from the stored residual
+                                images of those differences, one extra pass); 0 = the polynomial
+                                extrapolation alone.  Default 4 */
 } qms_desc;
 
 typedef struct {
@@ -136,6 +141,10 @@ typedef struct {
     unsigned status;         /* QMS_STATUS_* bits */
     int step_graph;          /* 1 when the step ran as one CUDA graph (start, residual and its refinement
                                 cycles behind a device-side convergence test), 0 otherwise */
+    int start_ls;            /* directions of the least-squares start of this step (0: none) */
+    double start_coef[4];    /* its start x_n + sum_j start_coef[j] (x_(n-j) - x_(n-j-1)), j = 0..3 */
+    double start_base;       /* |r|^2 of the polynomial start it improved on, and the |r|^2 the */
+    double start_pred;       /* least-squares solve predicted (unscaled sums of squares) */
 } qms_stats;
 
 typedef struct qms_handle qms_handle;

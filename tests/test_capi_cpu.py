@@ -110,7 +110,7 @@ def test_default_descriptor(lib):
     assert (d.dx, d.dy, d.dz, d.dt) == (1e-3, 2e-3, 3e-3, 1e-5)
     assert d.tol == 2e-13 and d.gmres_m == 32 and d.max_outer == 60
     assert d.mg_sweeps == 3 and d.mg_omega == 0.85 and d.mg_alpha == 1.5
-    assert d.mg_coupling == 1 and d.extrapolate == 3 and d.gm_first_extend == 0
+    assert d.mg_coupling == 1 and d.extrapolate == 3 and d.gm_first_extend == 0 and d.start_ls == 4
 
 
 def test_noalloc_size_query(lib):

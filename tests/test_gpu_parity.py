@@ -447,7 +447,7 @@ def test_extrapolated_start_residual_by_linearity(order):
     from alpineqms_gb300.inputs import Trajectory
     sched = VelocitySchedule([Trajectory(1, *t) for t in p["traj"]], p["dt"])
     s = solver_for(p["xs"], p["ys"], p["zs"], (p["dx"], p["dy"], p["dz"]), p["dt"], geom, p["props"],
-                   precision="mixed", extrapolate=order)
+                   precision="mixed", extrapolate=order, start_ls=0)
     B, G = np.asarray(p["B"], np.float64), np.asarray(p["G"], np.float64).ravel()
     s.steady(sched.steady(), B, G)
     v = sched.step(1)                    # one constant frame velocity: every step has the same operator
@@ -476,6 +476,51 @@ def test_extrapolated_start_residual_by_linearity(order):
     s.close()
     assert exact0 > 0
     assert abs(st["r0"] - exact0) <= 1e-3 * exact0 + 1e-15, (st["r0"], exact0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nls", [1, 2, 4])
+def test_least_squares_start(nls):
+    """With the least-squares start the first residual of a chained step is that of x_n plus the
+    reported combination of the last state differences: it must equal the exact FP64 residual of
+    that start state (rebuilt here from the returned solutions), be no larger than the residual
+    of the polynomial start of the same history, and every step must reach the tolerance with a
+    final residual that agrees with the exact one."""
+    p, geom = _conductor_case(True)
+    from alpineqms_gb300.trajectory import VelocitySchedule
+    from alpineqms_gb300.inputs import Trajectory
+    sched = VelocitySchedule([Trajectory(1, *t) for t in p["traj"]], p["dt"])
+    s = solver_for(p["xs"], p["ys"], p["zs"], (p["dx"], p["dy"], p["dz"]), p["dt"], geom, p["props"],
+                   precision="mixed", start_ls=nls)
+    B, G = np.asarray(p["B"], np.float64), np.asarray(p["G"], np.float64).ravel()
+    s.steady(sched.steady(), B, G)
+    v = sched.step(1)
+    X, S = [], []
+    for n in range(1, 11):
+        st = s.step(v, B, G)
+        assert st["status"] == 0, (n, st)
+        exact = s.residual_norm(True, v)
+        assert abs(st["r"] - exact) <= 0.25 * exact + 5e-15, (n, st["r"], exact)
+        X.append(s.get_state())
+        S.append(st)
+    st = S[-1]
+    assert st["start_ls"] == nls, st
+    gam = st["start_coef"]
+    assert all(np.isfinite(gam)) and all(gam[j] == 0.0 for j in range(nls, 4)), gam
+    # the start of the last step, rebuilt: x_n = X[-2], the differences before it
+    x_start = X[-2].copy()
+    for j in range(nls):
+        x_start += gam[j] * (X[-2 - j] - X[-3 - j])
+    cubic = 4.0 * (X[-2] + X[-4]) - 6.0 * X[-3] - X[-5]
+    s.set_state(x_start)                 # b is still the last step's
+    exact0 = s.residual_norm(True, v)
+    s.set_state(cubic)
+    exact_cubic = s.residual_norm(True, v)
+    s.close()
+    assert abs(st["r0"] - exact0) <= 1e-3 * exact0 + 1e-15, (st["r0"], exact0)
+    if nls >= 3:
+        assert exact0 <= 1.01 * exact_cubic, (exact0, exact_cubic)
+    assert st["start_pred"] <= 1.001 * st["start_base"], st
 
 
 @pytest.mark.gpu
