@@ -375,7 +375,7 @@ struct QStartRhs {
 // float and across the block in double: the solve only needs the coefficients to a few digits,
 // because the apply pass forms the residual of the start it writes exactly (by linearity).
 template <bool LS>
-__global__ void __launch_bounds__(256) qk_step_start(
+__global__ void __launch_bounds__(256, 4) qk_step_start(
     QGrid g, qdf* __restrict__ rfin, const double* b_a, const double* bprev_a, const qdf* __restrict__ dinv,
     qdf* __restrict__ r0, double* __restrict__ x, const double* xo1_a, const double* xo2_a, const double* xo3_a,
     const int xo, qdf* wnew_a, const qdf* w1_a, const qdf* w2_a, float* __restrict__ rfloat,
@@ -459,15 +459,18 @@ __global__ void __launch_bounds__(256) qk_step_start(
         r0[pl] = a;
         if (R.x0) R.x0[ref] = xs;
         if constexpr (LS) {
-            // xo = ls >= 1 directions; wnew is formed (w)
+            // xo = ls >= 1 directions; wnew is formed (w).  The differences in float from both
+            // words (consecutive w agree to a few per cent, so each word's difference is nearly
+            // exact): the sums only steer the coefficients
             const qdf v1 = xo >= 2 ? w1[pl] : qdf(), v2 = xo >= 3 ? w2[pl] : qdf(), v3 = xo >= 4 ? w3[pl] : qdf();
-            const qdf e1 = v1 - v2, e2 = e1 - (v2 - v3);          // w1 - w2, w1 - 2 w2 + w3
-            const qdf u2 = w - v1, u3 = u2 - e1, u4 = u3 - e2;
-            qdf base_r = a - w;
-            if (xo >= 2) base_r = base_r - u2;
-            if (xo >= 3) base_r = base_r - u3;
-            const float u[4] = {w.h, xo >= 2 ? u2.h : 0.f, xo >= 3 ? u3.h : 0.f, xo >= 4 ? u4.h : 0.f};
-            const float rb = base_r.h;
+            const float d1 = (w.h - v1.h) + (w.l - v1.l);        // w - w1
+            const float d2 = (v1.h - v2.h) + (v1.l - v2.l);      // w1 - w2
+            const float d3 = (v2.h - v3.h) + (v2.l - v3.l);      // w2 - w3
+            const float u2 = d1, u3 = d1 - d2, u4 = (d1 - d2) - (d2 - d3);
+            float rb = (a.h - w.h) + (a.l - w.l);
+            if (xo >= 2) rb -= u2;
+            if (xo >= 3) rb -= u3;
+            const float u[4] = {w.h + w.l, xo >= 2 ? u2 : 0.f, xo >= 3 ? u3 : 0.f, xo >= 4 ? u4 : 0.f};
             int q = 0;
 #pragma unroll
             for (int i0 = 0; i0 < 4; i0++)
@@ -626,6 +629,8 @@ __global__ void __launch_bounds__(256) qk_start_apply(
     const qdf* __restrict__ w3 = dp ? dp->w3 : w3_a;
     const double g1 = coef[0], g2 = coef[1], g3 = coef[2], g4 = coef[3];
     const qdf q1 = qdf_split(g1), q2 = qdf_split(g2), q3 = qdf_split(g3), q4 = qdf_split(g4);
+    // x_n + sum_j g_j d_j as one combination of the states (FP64 issue is scarce on GB300)
+    const double c0 = 1.0 + g1, c1 = g2 - g1, c2 = g3 - g2, c3 = g4 - g3, c4 = -g4;
     float racc = 0.f, xacc = 0.f;
     for (unsigned base = blockIdx.x * 64u; base < Nn; base += gridDim.x * 64u) {
         const unsigned t = base + lane;
@@ -647,18 +652,11 @@ __global__ void __launch_bounds__(256) qk_start_apply(
         const qdf r = r0[pl] - s;
         double xs = x[ref];
         if (!fix) {
-            const double x1 = xo1[ref];
-            double dx = g1 * (xs - x1);
-            if (ls >= 2) {
-                const double x2 = xo2[ref];
-                dx = fma(g2, x1 - x2, dx);
-                if (ls >= 3) {
-                    const double x3 = xo3[ref];
-                    dx = fma(g3, x2 - x3, dx);
-                    if (ls >= 4) dx = fma(g4, x3 - xo4[ref], dx);
-                }
-            }
-            xs += dx;
+            double t = c1 * xo1[ref];
+            if (ls >= 2) t = fma(c2, xo2[ref], t);
+            if (ls >= 3) t = fma(c3, xo3[ref], t);
+            if (ls >= 4) t = fma(c4, xo4[ref], t);
+            xs = fma(c0, xs, t);
             x[ref] = xs;
         }
         rfloat[pl] = r.h;
@@ -948,6 +946,20 @@ void qms_launch_extrapolate(const QGrid& g, double* x, const double* xold, const
     qk_extrapolate<<<qms_node_grid(g), qms_node_block(), 0, st>>>(g, x, xold, xold2, xold3, order);
 }
 
+// blocks of the least-squares start's first pass that are resident at once on the device
+static long long qms_step_start_ls_blocks() {
+    static std::atomic<long long> cached{0};
+    long long c = cached.load();
+    if (c > 0) return c;
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, qk_step_start<true>, 256, 0);
+    c = (long long)std::max(1, sms) * std::max(1, per);
+    cached.store(c);
+    return c;
+}
+
 void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const double* bprev, const qdf* dinv, qdf* r0,
                            const QStepStart& h, float* rfloat, double* partials, long long nb, cudaStream_t st,
                            const QStepPtrs* dptrs) {
@@ -962,9 +974,12 @@ void qms_launch_step_start(const QGrid& g, qdf* rfin, const double* b, const dou
         R.x0 = h.x0;
     }
     if (h.ls > 0) {
-        qk_step_start<true><<<(unsigned)nb, 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3, h.ls,
-                                                           h.wnew, h.w1, h.w2, nullptr, partials, R, dptrs, h.w3, h.lsp);
-        qk_ls_solve<<<1, 256, 0, st>>>(h.lsp, nb, h.ls, h.lsg);
+        // the first pass: one resident wave of blocks (fewer block sums to form and to add up)
+        const long long nb1 = std::min(nb, qms_step_start_ls_blocks());
+        qk_step_start<true><<<(unsigned)nb1, 256, 0, st>>>(g, rfin, b, bprev, dinv, r0, h.x, h.xo1, h.xo2, h.xo3, h.ls,
+                                                            h.wnew, h.w1, h.w2, nullptr, partials, R, dptrs, h.w3,
+                                                            h.lsp);
+        qk_ls_solve<<<1, 256, 0, st>>>(h.lsp, nb1, h.ls, h.lsg);
         qk_start_apply<<<(unsigned)nb, 256, 0, st>>>(g, h.x, h.xo1, h.xo2, h.xo3, h.xo4, h.ls, r0, h.wnew, h.w1, h.w2,
                                                      h.w3, h.lsg, rfin, rfloat, partials, dptrs);
         return;
