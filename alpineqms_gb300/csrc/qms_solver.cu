@@ -1679,13 +1679,14 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
     // second replay raised it instead: one slow step pinned it at 7-8 for 32 solves.)
     // After a least-squares start the start residual is within a few times the tolerance and
     // falls from step to step, so the count follows the measured rate: a one-replay solve that
-    // ended below tol / 2 takes the count that this solve's reduction per FGMRES step says
-    // reaches tol / 2 from its start (at least one less); a solve that needed a second replay
+    // ended below tol / 4 takes the count that this solve's reduction per FGMRES step says
+    // reaches tol / 4 from its start (at least one less); a solve that needed a second replay
     // goes up by one (two after a third), and when its start had every direction it holds there
     // for 4 solves (the first steps of a run know fewer directions and start worse: floors from
     // them kept the count high well after).  Floors set by solves without this start do not apply.
-    // (Targets of tol / 10 and tol / 4 ran 26.80 and 25.51 ms per step on steps 6-25 of the
-    // moving plate at 256^3, against 24.74 ms: the extra second cycles cost less than the margin.)
+    // (On steps 6-25 of the moving plate at 256^3, targets of tol / 10, tol / 4 and tol / 2 ran
+    // 26.80, 25.51 and 24.74 ms per step; tol / 2 left the field 1.05e-8 from the plain FP64
+    // solve's at one step of 200, tol / 4 at most 9.8e-9.)
     if (graph_cycles > 0 && rel <= desc.tol && ls > 0) {
         if (gm_ls_floor > 0 && ++gm_ls_floor_age > 4) { gm_ls_floor = 0; gm_ls_floor_age = 0; }
         if (graph_cycles >= 2) {
@@ -1694,12 +1695,12 @@ int QmsSolver::solve(bool transient, const double v[3], const double B[3], const
                 gm_ls_floor = gm_k_est;
                 gm_ls_floor_age = 0;
             }
-        } else if (rel < desc.tol / 2.0) {
+        } else if (rel < desc.tol / 4.0) {
             const double r0 = stats.initial_residual;
             int need = 1;
-            if (r0 > desc.tol / 2.0 && rel > 0.0 && r0 > rel) {
+            if (r0 > desc.tol / 4.0 && rel > 0.0 && r0 > rel) {
                 const double rate = std::log(r0 / rel) / std::max(1, gm_k_est);
-                need = (int)std::ceil(std::log(r0 / (desc.tol / 2.0)) / rate);
+                need = (int)std::ceil(std::log(r0 / (desc.tol / 4.0)) / rate);
             }
             gm_k_est = std::max(std::max(1, gm_ls_floor), std::min(gm_k_est - 1, need));
         }
