@@ -511,7 +511,7 @@ def run_gpu(args):
                                       "gmres_m": desc.gmres_m, "mg_sweeps": desc.mg_sweeps,
                                       "mg_omega": desc.mg_omega, "mg_alpha": desc.mg_alpha,
                                       "mg_coupling": "lower block-triangular" if desc.mg_coupling == 1
-                                      else "block-diagonal", "extrapolate": desc.extrapolate,
+                                      else "block-diagonal", "extrapolate": desc.extrapolate, "start_ls": desc.start_ls,
                                       "residual": "FP64 anchor + double-float" if args.precision == "mixed"
                                       else "FP64"},
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
