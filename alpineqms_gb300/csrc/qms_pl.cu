@@ -371,9 +371,10 @@ struct QStartRhs {
 // (the residual images of d_n and of its backward differences: nearly independent, unlike the
 // w themselves), the Gram matrix u_i . u_j, the products u_i . r_b with the residual r_b of the
 // polynomial start of order min(ls, 3) (r_b = r0 - u1 - u2 - u3), and r_b . r_b, into lsp
-// (QMS_LS_SUMS x nb, quantity-major).  Products of the float high words, summed per thread in
-// float and across the block in double: the solve only needs the coefficients to a few digits,
-// because the apply pass forms the residual of the start it writes exactly (by linearity).
+// (QMS_LS_SUMS x nb, quantity-major).  The basis and r_b in float (from both words of each
+// double-float value), products summed per thread in float and across the block in double: the
+// solve only needs the coefficients to a few digits, because the apply pass forms the residual
+// of the start it writes exactly (by linearity).  The launch is one resident wave of blocks.
 template <bool LS>
 __global__ void __launch_bounds__(256, 4) qk_step_start(
     QGrid g, qdf* __restrict__ rfin, const double* b_a, const double* bprev_a, const qdf* __restrict__ dinv,
